@@ -1,0 +1,719 @@
+// C ABI implementation (include/lbm_gb300.h): handle lifetime, geometry,
+// initialisation, the time loop and readouts.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gb300.h"
+#include "lbm_aux.cuh"
+#include "lbm_dispatch.cuh"
+#include "lbm_f64x.cuh"
+
+using namespace lbm;
+
+struct lbm_handle {
+   lbm_config cfg;
+   int Q = 19;
+   int storage = ST_F64;
+   int arith = AR_F64X;
+   int elem = 8;
+   int64_t ncell = 0, nfluid = 0, plane = 0, t = 0;
+   uint64_t buffer_bytes = 0, device_bytes = 0;
+   void* buf[2] = {nullptr, nullptr};
+   int cur = 0;                    // AB: buffer holding the latest state
+   uint32_t* links = nullptr;      // null when the box is fully periodic and has no solids
+   uint8_t* solid_dev = nullptr;   // scratch for building links
+   double* force_field = nullptr;  // planar [3][plane]
+   float* force_field_f = nullptr;
+   double* porosity = nullptr;
+   float* porosity_f = nullptr;
+   double* staging = nullptr;      // one dense double plane
+   double* partials = nullptr;     // reduction scratch: kReduceBlocks * 4 doubles
+   double* reduce_out = nullptr;   // 4 doubles
+   cudaStream_t stream = nullptr;
+   std::string err;
+};
+
+namespace {
+
+constexpr int kReduceBlocks = 152 * 8;
+
+lbm_status fail(lbm_handle* h, lbm_status s, const char* fmt, ...)
+{
+   if (h) {
+      char buf[512];
+      va_list ap;
+      va_start(ap, fmt);
+      vsnprintf(buf, sizeof(buf), fmt, ap);
+      va_end(ap);
+      h->err = buf;
+   }
+   return s;
+}
+
+lbm_status cuda_fail(lbm_handle* h, cudaError_t e, const char* what)
+{
+   return fail(h, LBM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define LBM_CUDA(h, call)                                            \
+   do {                                                              \
+      cudaError_t e_ = (call);                                       \
+      if (e_ != cudaSuccess) return cuda_fail((h), e_, #call);       \
+   } while (0)
+
+GridDims dims_of(const lbm_handle* h)
+{
+   GridDims g;
+   g.nx = h->cfg.nx;
+   g.ny = h->cfg.ny;
+   g.nz = h->cfg.nz;
+   g.ncell = h->ncell;
+   g.plane = h->plane;
+   for (int d = 0; d < 3; d++) g.periodic[d] = h->cfg.periodic[d] ? 1 : 0;
+   return g;
+}
+
+unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+bool fully_periodic(const lbm_handle* h)
+{
+   return h->cfg.periodic[0] && h->cfg.periodic[1] && h->cfg.periodic[2];
+}
+
+lbm_status dev_alloc(lbm_handle* h, void** p, size_t bytes)
+{
+   if (h->cfg.max_device_bytes && h->device_bytes + bytes > h->cfg.max_device_bytes)
+      return fail(h, LBM_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes exceeds max_device_bytes=%llu",
+                  bytes, (unsigned long long)h->cfg.max_device_bytes);
+   cudaError_t e = cudaMalloc(p, bytes);
+   if (e != cudaSuccess) {
+      cudaGetLastError();
+      *p = nullptr;
+      return fail(h, LBM_ERR_OUT_OF_MEMORY, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+   }
+   h->device_bytes += bytes;
+   return LBM_OK;
+}
+
+void dev_free(lbm_handle* h, void* p, size_t bytes)
+{
+   if (!p) return;
+   cudaFree(p);
+   h->device_bytes -= std::min<uint64_t>(h->device_bytes, bytes);
+}
+
+// Step-kernel parameters for the cell range [start, end).
+KParams make_params(const lbm_handle* h, int64_t start, int64_t end, Launch& L)
+{
+   KParams p;
+   std::memset(&p, 0, sizeof(p));
+   const lbm_config& c = h->cfg;
+   p.nx = c.nx;
+   p.ny = c.ny;
+   p.nz = c.nz;
+   p.ncell = h->ncell;
+   p.plane = h->plane;
+   p.cstart = start;
+   p.cend = end;
+   const int64_t nxy = (int64_t)c.nx * c.ny;
+   const int64_t z0 = start / nxy, z1 = (end - 1) / nxy + 1;
+   p.z0 = (int)z0;
+   p.omega = c.omega;
+   p.om1 = 1.0 - c.omega;
+   p.om2 = 1.0 - 0.5 * c.omega;
+   p.omegaf = (float)p.omega;
+   p.om1f = (float)p.om1;
+   p.om2f = (float)p.om2;
+   for (int d = 0; d < 3; d++) {
+      p.F[d] = c.force[d];
+      p.Ff[d] = (float)c.force[d];
+   }
+   p.compat = (c.unroll && h->Q == 19 && c.prop_pattern == LBM_PATTERN_AA) ? 1 : 0;
+   p.links = h->links;
+   p.force_field = h->force_field;
+   p.force_field_f = h->force_field_f;
+   p.porosity = h->porosity;
+   p.porosity_f = h->porosity_f;
+   auto split = [](double d, float* out) {
+      const float hi = (float)d;
+      out[0] = hi;
+      out[1] = (float)(d - (double)hi);
+   };
+   split(p.om1, p.x_om1);
+   split(p.omega, p.x_omega);
+   for (int k = 0; k < 4; k++) {
+      double w;
+      if (h->Q == 19) w = k == 0 ? 1.0 / 3.0 : (k == 1 ? 1.0 / 18.0 : 1.0 / 36.0);
+      else w = k == 0 ? 8.0 / 27.0 : (k == 1 ? 2.0 / 27.0 : (k == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+      split(c.omega * w, p.x_ow[k]);
+   }
+   for (int d = 0; d < 3; d++) split(c.force[d], p.x_F[d]);
+   int bx = (int)std::min<int64_t>(256, ((c.nx + 31) / 32) * 32);
+   L.block = dim3(bx, 1, 1);
+   L.grid = dim3((c.nx + bx - 1) / bx, c.ny, (unsigned)(z1 - z0));
+   L.stream = h->stream;
+   return p;
+}
+
+lbm_status launch(lbm_handle* h, int kind, const void* src, void* dst, int64_t start, int64_t count)
+{
+   if (count <= 0) return LBM_OK;
+   Launch L;
+   const KParams p = make_params(h, start, start + count, L);
+   const bool links = h->links != nullptr;
+   const bool fields = h->force_field || h->force_field_f || h->porosity || h->porosity_f;
+   cudaError_t e;
+   if (h->Q == 19) {
+      e = h->storage == ST_F64 ? launch_step_q19_f64(h->arith, kind, L, p, src, dst, links, fields)
+                               : launch_step_q19_low(h->storage, kind, L, p, src, dst, links, fields);
+   } else {
+      e = h->storage == ST_F64 ? launch_step_q27_f64(h->arith, kind, L, p, src, dst, links, fields)
+                               : launch_step_q27_low(h->storage, kind, L, p, src, dst, links, fields);
+   }
+   if (e != cudaSuccess) return cuda_fail(h, e, "step kernel launch");
+   return LBM_OK;
+}
+
+template <template <int, int> class F, typename... A>
+void dispatch_q_st(int Q, int st, A&&... a)
+{
+   if (Q == 19) {
+      switch (st) {
+         case ST_F64: F<19, ST_F64>::run(a...); break;
+         case ST_F32: F<19, ST_F32>::run(a...); break;
+         case ST_BF16: F<19, ST_BF16>::run(a...); break;
+         default: F<19, ST_F16>::run(a...); break;
+      }
+   } else {
+      switch (st) {
+         case ST_F64: F<27, ST_F64>::run(a...); break;
+         case ST_F32: F<27, ST_F32>::run(a...); break;
+         case ST_BF16: F<27, ST_BF16>::run(a...); break;
+         default: F<27, ST_F16>::run(a...); break;
+      }
+   }
+}
+
+template <int Q, int ST>
+struct InitEq {
+   static void run(const lbm_handle* h, const double* rho, const double* u, int aa)
+   {
+      init_eq_kernel<Q, ST><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(dims_of(h), rho, u, h->buf[0],
+                                                                               h->buf[1], aa);
+   }
+};
+
+template <int Q, int ST>
+struct ImportPlane {
+   static void run(const lbm_handle* h, int slot, double w, void* b0, void* b1)
+   {
+      import_plane_kernel<ST><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(dims_of(h), h->staging, slot, w,
+                                                                                 b0, b1);
+   }
+};
+
+template <int Q, int ST>
+struct ExportPlane {
+   static void run(const lbm_handle* h, const void* buf, int s, int mode)
+   {
+      export_plane_kernel<Q, ST><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(dims_of(h), buf, h->links, s,
+                                                                                    mode, h->staging);
+   }
+};
+
+template <int Q, int ST>
+struct Macros {
+   static void run(const lbm_handle* h, const void* buf, int mode, double* rho, double* u)
+   {
+      macros_kernel<Q, ST><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(dims_of(h), buf, h->links, mode,
+                                                                              rho, u);
+   }
+};
+
+template <int Q, int ST>
+struct Conserved {
+   static void run(const lbm_handle* h, const void* buf, int mode, double* partials, double* out)
+   {
+      conserved_partial_kernel<Q, ST><<<kReduceBlocks, kReduceThreads, 0, h->stream>>>(dims_of(h), buf, h->links,
+                                                                                         mode, partials);
+      conserved_final_kernel<<<1, kReduceThreads, 0, h->stream>>>(partials, kReduceBlocks, out);
+   }
+};
+
+double weight(int Q, int s)
+{
+   const int n2 = lat_norm2(Q, s);
+   if (Q == 19) return n2 == 0 ? 1.0 / 3.0 : (n2 == 1 ? 1.0 / 18.0 : 1.0 / 36.0);
+   return n2 == 0 ? 8.0 / 27.0 : (n2 == 1 ? 2.0 / 27.0 : (n2 == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+}
+
+// Buffer the reference reads back, and how its slots map to directions.
+const void* readout_buffer(const lbm_handle* h)
+{
+   return h->cfg.prop_pattern == LBM_PATTERN_AA ? h->buf[0] : h->buf[h->cur];
+}
+
+// Export mode for logical populations: 0 stored slot s, 1 own slot opp(s),
+// 2 pull gather.
+int logical_mode(const lbm_handle* h)
+{
+   if (h->cfg.prop_pattern == LBM_PATTERN_AA) return (h->t % 2 == 0) ? 1 : 2;
+   return h->cfg.pull ? 2 : 0;
+}
+
+lbm_status check_handle(const lbm_handle* h) { return h ? LBM_OK : LBM_ERR_INVALID_ARGUMENT; }
+
+}  // namespace
+
+extern "C" {
+
+const char* lbm_status_string(lbm_status s)
+{
+   switch (s) {
+      case LBM_OK: return "ok";
+      case LBM_ERR_INVALID_ARGUMENT: return "invalid argument";
+      case LBM_ERR_OUT_OF_MEMORY: return "out of device memory";
+      case LBM_ERR_CUDA: return "CUDA error";
+      case LBM_ERR_DIVERGED: return "diverged (non-finite conserved sums)";
+      case LBM_ERR_UNSUPPORTED: return "unsupported";
+      case LBM_ERR_STATE: return "invalid state";
+   }
+   return "unknown status";
+}
+
+const char* lbm_last_error(const lbm_handle* h)
+{
+   if (!h) return "null handle";
+   return h->err.c_str();
+}
+
+lbm_status lbm_config_default(lbm_config* cfg)
+{
+   if (!cfg) return LBM_ERR_INVALID_ARGUMENT;
+   std::memset(cfg, 0, sizeof(*cfg));
+   cfg->lattice = 19;
+   cfg->prop_pattern = LBM_PATTERN_AA;
+   cfg->nx = cfg->ny = cfg->nz = 16;
+   cfg->periodic[0] = cfg->periodic[1] = cfg->periodic[2] = 1;
+   cfg->omega = 1.0;
+   cfg->force[0] = 0.000001;
+   cfg->storage = LBM_STORE_F64;
+   cfg->arithmetic = LBM_ARITH_AUTO;
+   return LBM_OK;
+}
+
+void lbm_destroy(lbm_handle* h)
+{
+   if (!h) return;
+   int prev = -1;
+   cudaGetDevice(&prev);
+   cudaSetDevice(h->cfg.device);
+   if (h->stream) cudaStreamSynchronize(h->stream);
+   cudaFree(h->buf[0]);
+   cudaFree(h->buf[1]);
+   cudaFree(h->links);
+   cudaFree(h->solid_dev);
+   cudaFree(h->force_field);
+   cudaFree(h->force_field_f);
+   cudaFree(h->porosity);
+   cudaFree(h->porosity_f);
+   cudaFree(h->staging);
+   cudaFree(h->partials);
+   cudaFree(h->reduce_out);
+   if (prev >= 0) cudaSetDevice(prev);
+   delete h;
+}
+
+lbm_status lbm_create(const lbm_config* cfg, lbm_handle** out)
+{
+   if (!cfg || !out) return LBM_ERR_INVALID_ARGUMENT;
+   *out = nullptr;
+   lbm_handle* h = new (std::nothrow) lbm_handle;
+   if (!h) return LBM_ERR_OUT_OF_MEMORY;
+   h->cfg = *cfg;
+   lbm_status st = LBM_OK;
+   const lbm_config& c = *cfg;
+   const int64_t ncell = (int64_t)c.nx * c.ny * c.nz;
+   if (c.lattice != 19 && c.lattice != 27) st = fail(h, LBM_ERR_INVALID_ARGUMENT, "lattice must be 19 or 27");
+   else if (c.nx < 1 || c.ny < 1 || c.nz < 1 || c.ny > 65535 || c.nz > 65535)
+      st = fail(h, LBM_ERR_INVALID_ARGUMENT, "grid dimensions out of range (ny, nz <= 65535)");
+   else if (ncell > (int64_t)INT32_MAX)
+      st = fail(h, LBM_ERR_INVALID_ARGUMENT, "nx*ny*nz must be below 2^31 cells");
+   else if (c.prop_pattern != LBM_PATTERN_AA && c.prop_pattern != LBM_PATTERN_AB)
+      st = fail(h, LBM_ERR_INVALID_ARGUMENT, "prop_pattern must be 0 (AB) or 1 (AA)");
+   else if (c.storage < LBM_STORE_F64 || c.storage > LBM_STORE_F16)
+      st = fail(h, LBM_ERR_INVALID_ARGUMENT, "unknown storage");
+   else if (!(c.omega > 0.0 && c.omega < 2.0))
+      st = fail(h, LBM_ERR_INVALID_ARGUMENT, "omega must lie in (0, 2)");
+   else if (c.arithmetic < LBM_ARITH_AUTO || c.arithmetic > LBM_ARITH_F32)
+      st = fail(h, LBM_ERR_INVALID_ARGUMENT, "unknown arithmetic");
+   if (st == LBM_OK) {
+      h->Q = c.lattice;
+      h->storage = c.storage;
+      if (c.storage == LBM_STORE_F64) {
+         h->arith = (c.arithmetic == LBM_ARITH_F64) ? AR_F64 : AR_F64X;
+         if (c.arithmetic == LBM_ARITH_F32)
+            st = fail(h, LBM_ERR_UNSUPPORTED, "FP64 storage computes in F64 or F64X arithmetic");
+      } else {
+         h->arith = AR_F32;
+         if (c.arithmetic == LBM_ARITH_F64 || c.arithmetic == LBM_ARITH_F64X)
+            st = fail(h, LBM_ERR_UNSUPPORTED, "shifted FP32/BF16/FP16 storage computes in FP32");
+      }
+      h->elem = c.storage == LBM_STORE_F64 ? 8 : (c.storage == LBM_STORE_F32 ? 4 : 2);
+      h->ncell = ncell;
+      h->nfluid = ncell;
+      // Planes start on 512-byte boundaries.
+      const int64_t align = 512 / h->elem;
+      h->plane = (ncell + align - 1) / align * align;
+      h->buffer_bytes = (uint64_t)h->plane * h->Q * h->elem;
+   }
+   if (st == LBM_OK) {
+      int ndev = 0;
+      cudaError_t e = cudaGetDeviceCount(&ndev);
+      if (e != cudaSuccess || c.device < 0 || c.device >= ndev)
+         st = fail(h, LBM_ERR_CUDA, "no CUDA device %d (%s)", c.device, cudaGetErrorString(e));
+      else if ((e = cudaSetDevice(c.device)) != cudaSuccess)
+         st = cuda_fail(h, e, "cudaSetDevice");
+   }
+   if (st == LBM_OK) st = dev_alloc(h, &h->buf[0], h->buffer_bytes);
+   if (st == LBM_OK && c.prop_pattern == LBM_PATTERN_AB) st = dev_alloc(h, &h->buf[1], h->buffer_bytes);
+   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->staging, sizeof(double) * (size_t)h->ncell);
+   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->partials, sizeof(double) * 4 * kReduceBlocks);
+   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->reduce_out, sizeof(double) * 4);
+   if (st == LBM_OK) st = lbm_set_solid(h, nullptr);
+   if (st == LBM_OK) st = lbm_init_equilibrium(h, nullptr, nullptr);
+   if (st != LBM_OK) {
+      std::string msg = h->err;
+      lbm_destroy(h);
+      fprintf(stderr, "lbm_create: %s\n", msg.c_str());
+      return st;
+   }
+   *out = h;
+   return LBM_OK;
+}
+
+lbm_status lbm_get_info(const lbm_handle* h, lbm_info* info)
+{
+   if (!h || !info) return LBM_ERR_INVALID_ARGUMENT;
+   info->ncell = h->ncell;
+   info->nfluid = h->nfluid;
+   info->time_step = h->t;
+   info->plane_stride = h->plane;
+   info->buffer_bytes = h->buffer_bytes;
+   info->device_bytes = h->device_bytes;
+   info->bytes_per_update = 2 * h->Q * h->elem;
+   info->lattice = h->Q;
+   info->storage = h->storage;
+   info->arithmetic = h->arith == AR_F64 ? LBM_ARITH_F64 : (h->arith == AR_F64X ? LBM_ARITH_F64X : LBM_ARITH_F32);
+   return LBM_OK;
+}
+
+lbm_status lbm_set_stream(lbm_handle* h, void* stream)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   h->stream = static_cast<cudaStream_t>(stream);
+   return LBM_OK;
+}
+
+lbm_status lbm_synchronize(lbm_handle* h)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   return LBM_OK;
+}
+
+lbm_status lbm_set_solid(lbm_handle* h, const uint8_t* solid)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   int64_t nsolid = 0;
+   if (solid)
+      for (int64_t c = 0; c < h->ncell; c++) nsolid += solid[c] ? 1 : 0;
+   h->nfluid = h->ncell - nsolid;
+   const bool need_links = nsolid > 0 || !fully_periodic(h);
+   if (!need_links) {
+      dev_free(h, h->links, sizeof(uint32_t) * (size_t)h->ncell);
+      h->links = nullptr;
+      return LBM_OK;
+   }
+   if (!h->links) {
+      lbm_status st = dev_alloc(h, (void**)&h->links, sizeof(uint32_t) * (size_t)h->ncell);
+      if (st != LBM_OK) return st;
+   }
+   uint8_t* sd = nullptr;
+   if (solid) {
+      lbm_status st = dev_alloc(h, (void**)&sd, (size_t)h->ncell);
+      if (st != LBM_OK) return st;
+      LBM_CUDA(h, cudaMemcpyAsync(sd, solid, (size_t)h->ncell, cudaMemcpyHostToDevice, h->stream));
+   }
+   const GridDims g = dims_of(h);
+   if (h->Q == 19) build_links_kernel<19><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(g, sd, h->links);
+   else build_links_kernel<27><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(g, sd, h->links);
+   LBM_CUDA(h, cudaGetLastError());
+   LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   dev_free(h, sd, (size_t)h->ncell);
+   return LBM_OK;
+}
+
+lbm_status lbm_geometry_cylinder(double simulation_size, int dims[3], uint8_t* solid)
+{
+   // src/geometries/Geometry.cpp:59-71 (lengths) and :112-140 (mask): radius
+   // and axial length truncated to int; a cell is fluid when
+   // int(distance to the axis) <= radius, the axis at radius + 1.5.
+   if (!dims || !(simulation_size > 0.0)) return LBM_ERR_INVALID_ARGUMENT;
+   const int radius = (int)(8.0 * simulation_size);
+   const int axial = (int)(84.0 * simulation_size);
+   if (radius < 1 || axial < 1) return LBM_ERR_INVALID_ARGUMENT;
+   dims[0] = axial;
+   dims[1] = 2 * radius + 3;
+   dims[2] = 2 * radius + 3;
+   if (!solid) return LBM_OK;
+   const double r = (double)((dims[1] - 3) / 2);
+   const double axis = r + 1.5;
+   for (int k = 0; k < dims[2]; k++)
+      for (int j = 0; j < dims[1]; j++) {
+         const int dist = (int)std::sqrt(std::pow(j - axis, 2.0) + std::pow(k - axis, 2.0));
+         const uint8_t s = dist <= r ? 0 : 1;
+         for (int i = 0; i < dims[0]; i++) solid[(size_t)i + (size_t)dims[0] * ((size_t)j + (size_t)dims[1] * k)] = s;
+      }
+   return LBM_OK;
+}
+
+static lbm_status set_field(lbm_handle* h, const double* host, int ncomp, double** d64, float** d32)
+{
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   const size_t n = (size_t)h->plane * ncomp;
+   if (!host) {
+      dev_free(h, *d64, sizeof(double) * n);
+      dev_free(h, *d32, sizeof(float) * n);
+      *d64 = nullptr;
+      *d32 = nullptr;
+      return LBM_OK;
+   }
+   if (h->storage == ST_F64) {
+      if (!*d64) {
+         lbm_status st = dev_alloc(h, (void**)d64, sizeof(double) * n);
+         if (st != LBM_OK) return st;
+      }
+      for (int k = 0; k < ncomp; k++)
+         LBM_CUDA(h, cudaMemcpyAsync(*d64 + (size_t)k * h->plane, host + (size_t)k * h->ncell,
+                                     sizeof(double) * (size_t)h->ncell, cudaMemcpyHostToDevice, h->stream));
+   } else {
+      if (!*d32) {
+         lbm_status st = dev_alloc(h, (void**)d32, sizeof(float) * n);
+         if (st != LBM_OK) return st;
+      }
+      std::vector<float> tmp((size_t)h->ncell);
+      for (int k = 0; k < ncomp; k++) {
+         for (int64_t c = 0; c < h->ncell; c++) tmp[(size_t)c] = (float)host[(size_t)k * h->ncell + c];
+         LBM_CUDA(h, cudaMemcpy(*d32 + (size_t)k * h->plane, tmp.data(), sizeof(float) * (size_t)h->ncell,
+                                cudaMemcpyHostToDevice));
+      }
+   }
+   LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   return LBM_OK;
+}
+
+lbm_status lbm_set_force_field(lbm_handle* h, const double* field)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   return set_field(h, field, 3, &h->force_field, &h->force_field_f);
+}
+
+lbm_status lbm_set_porosity(lbm_handle* h, const double* porosity)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (porosity)
+      for (int64_t c = 0; c < h->ncell; c++)
+         if (!(porosity[c] >= 0.0 && porosity[c] <= 1.0))
+            return fail(h, LBM_ERR_INVALID_ARGUMENT, "porosity[%lld] = %g outside [0, 1]", (long long)c,
+                        porosity[c]);
+   return set_field(h, porosity, 1, &h->porosity, &h->porosity_f);
+}
+
+lbm_status lbm_init_equilibrium(lbm_handle* h, const double* rho, const double* u)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   double* drho = nullptr;
+   double* du = nullptr;
+   const size_t n = (size_t)h->ncell;
+   lbm_status st = LBM_OK;
+   if (rho) st = dev_alloc(h, (void**)&drho, sizeof(double) * n);
+   if (st == LBM_OK && u) st = dev_alloc(h, (void**)&du, sizeof(double) * 3 * n);
+   if (st == LBM_OK && rho)
+      LBM_CUDA(h, cudaMemcpyAsync(drho, rho, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
+   if (st == LBM_OK && u)
+      LBM_CUDA(h, cudaMemcpyAsync(du, u, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
+   if (st == LBM_OK) {
+      const int aa = h->cfg.prop_pattern == LBM_PATTERN_AA ? 1 : 0;
+      dispatch_q_st<InitEq>(h->Q, h->storage, h, drho, du, aa);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) st = cuda_fail(h, e, "init_eq_kernel");
+      else if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) st = cuda_fail(h, e, "init_eq sync");
+   }
+   dev_free(h, drho, sizeof(double) * n);
+   dev_free(h, du, sizeof(double) * 3 * n);
+   if (st == LBM_OK) {
+      h->t = 0;
+      h->cur = 0;
+   }
+   return st;
+}
+
+lbm_status lbm_set_populations(lbm_handle* h, const double* f, int layout)
+{
+   if (!h || !f || (layout != LBM_LAYOUT_RAW && layout != LBM_LAYOUT_LOGICAL)) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   const bool aa = h->cfg.prop_pattern == LBM_PATTERN_AA;
+   if (layout == LBM_LAYOUT_LOGICAL) {
+      h->t = 0;
+      h->cur = 0;
+   }
+   for (int s = 0; s < h->Q; s++) {
+      LBM_CUDA(h, cudaMemcpyAsync(h->staging, f + (size_t)s * h->ncell, sizeof(double) * (size_t)h->ncell,
+                                  cudaMemcpyHostToDevice, h->stream));
+      int slot = s;
+      void* b0 = aa ? h->buf[0] : h->buf[h->cur];
+      void* b1 = nullptr;
+      if (layout == LBM_LAYOUT_LOGICAL) {
+         if (aa) slot = lat_opp(h->Q, s);
+         else b1 = h->buf[1 - h->cur];
+      }
+      dispatch_q_st<ImportPlane>(h->Q, h->storage, h, slot, weight(h->Q, s), b0, b1);
+      LBM_CUDA(h, cudaGetLastError());
+   }
+   LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   return LBM_OK;
+}
+
+lbm_status lbm_get_populations(lbm_handle* h, double* f, int layout)
+{
+   if (!h || !f || (layout != LBM_LAYOUT_RAW && layout != LBM_LAYOUT_LOGICAL)) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   const int mode = layout == LBM_LAYOUT_RAW ? 0 : logical_mode(h);
+   const void* buf = readout_buffer(h);
+   for (int s = 0; s < h->Q; s++) {
+      dispatch_q_st<ExportPlane>(h->Q, h->storage, h, buf, s, mode);
+      LBM_CUDA(h, cudaGetLastError());
+      LBM_CUDA(h, cudaMemcpyAsync(f + (size_t)s * h->ncell, h->staging, sizeof(double) * (size_t)h->ncell,
+                                  cudaMemcpyDeviceToHost, h->stream));
+   }
+   LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   return LBM_OK;
+}
+
+lbm_status lbm_step(lbm_handle* h, int nsteps)
+{
+   if (!h || nsteps < 0) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   for (int i = 0; i < nsteps; i++) {
+      lbm_status st;
+      if (h->cfg.prop_pattern == LBM_PATTERN_AA) {
+         const int kind = (h->t % 2 == 0) ? K_AA_EVEN : K_AA_ODD;
+         st = launch(h, kind, h->buf[0], h->buf[0], 0, h->ncell);
+      } else {
+         const int kind = h->cfg.pull ? K_AB_PULL : K_AB_PUSH;
+         st = launch(h, kind, h->buf[h->cur], h->buf[1 - h->cur], 0, h->ncell);
+         h->cur = 1 - h->cur;
+      }
+      if (st != LBM_OK) return st;
+      h->t++;
+   }
+   return LBM_OK;
+}
+
+lbm_status lbm_get_macros(lbm_handle* h, double* rho, double* u)
+{
+   if (!h || !rho || !u) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   // The reference reads AA through the streamed populations and AB straight
+   // from the stored buffer (src/propagation/PropagationAB.cpp:222-281).
+   const int mode = h->cfg.prop_pattern == LBM_PATTERN_AA ? logical_mode(h) : 0;
+   double* dr = nullptr;
+   double* du = nullptr;
+   const size_t n = (size_t)h->ncell;
+   lbm_status st = dev_alloc(h, (void**)&dr, sizeof(double) * n);
+   if (st == LBM_OK) st = dev_alloc(h, (void**)&du, sizeof(double) * 3 * n);
+   if (st == LBM_OK) {
+      dispatch_q_st<Macros>(h->Q, h->storage, h, readout_buffer(h), mode, dr, du);
+      cudaError_t e = cudaGetLastError();
+      if (e == cudaSuccess) e = cudaMemcpyAsync(rho, dr, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(u, du, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+      if (e != cudaSuccess) st = cuda_fail(h, e, "lbm_get_macros");
+   }
+   dev_free(h, dr, sizeof(double) * n);
+   dev_free(h, du, sizeof(double) * 3 * n);
+   return st;
+}
+
+lbm_status lbm_reduce_conserved(lbm_handle* h, double out[4])
+{
+   if (!h || !out) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   dispatch_q_st<Conserved>(h->Q, h->storage, h, readout_buffer(h), logical_mode(h), h->partials,
+                            h->reduce_out);
+   LBM_CUDA(h, cudaGetLastError());
+   LBM_CUDA(h, cudaMemcpyAsync(out, h->reduce_out, sizeof(double) * 4, cudaMemcpyDeviceToHost, h->stream));
+   LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   for (int k = 0; k < 4; k++)
+      if (!std::isfinite(out[k])) return fail(h, LBM_ERR_DIVERGED, "conserved sum %d is %g", k, out[k]);
+   return LBM_OK;
+}
+
+static lbm_status check_range(lbm_handle* h, int64_t start, int64_t count)
+{
+   if (start < 0 || count < 0 || start + count > h->ncell)
+      return fail(h, LBM_ERR_INVALID_ARGUMENT, "cell range [%lld, %lld) outside [0, %lld)", (long long)start,
+                  (long long)(start + count), (long long)h->ncell);
+   return LBM_OK;
+}
+
+lbm_status lbm_timestep_even_force(lbm_handle* h, void* dstrb, int64_t start, int64_t count)
+{
+   if (!h || !dstrb) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->cfg.prop_pattern != LBM_PATTERN_AA) return fail(h, LBM_ERR_STATE, "handle is not configured for AA");
+   lbm_status st = check_range(h, start, count);
+   if (st != LBM_OK) return st;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   return launch(h, K_AA_EVEN, dstrb, dstrb, start, count);
+}
+
+lbm_status lbm_timestep_odd_force(lbm_handle* h, void* dstrb, int64_t start, int64_t count)
+{
+   if (!h || !dstrb) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->cfg.prop_pattern != LBM_PATTERN_AA) return fail(h, LBM_ERR_STATE, "handle is not configured for AA");
+   lbm_status st = check_range(h, start, count);
+   if (st != LBM_OK) return st;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   return launch(h, K_AA_ODD, dstrb, dstrb, start, count);
+}
+
+lbm_status lbm_timestep_force(lbm_handle* h, const void* src, void* tgt, int64_t start, int64_t count)
+{
+   if (!h || !src || !tgt || src == tgt) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->cfg.prop_pattern != LBM_PATTERN_AB) return fail(h, LBM_ERR_STATE, "handle is not configured for AB");
+   lbm_status st = check_range(h, start, count);
+   if (st != LBM_OK) return st;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   return launch(h, h->cfg.pull ? K_AB_PULL : K_AB_PUSH, src, tgt, start, count);
+}
+
+lbm_status lbm_population_buffer(lbm_handle* h, void** dev_ptr)
+{
+   if (!h || !dev_ptr) return LBM_ERR_INVALID_ARGUMENT;
+   *dev_ptr = const_cast<void*>(readout_buffer(h));
+   return LBM_OK;
+}
+
+}  // extern "C"

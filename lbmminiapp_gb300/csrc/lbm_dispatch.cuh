@@ -1,0 +1,59 @@
+// Launch dispatch for the step kernels: one translation unit per lattice and
+// storage group instantiates its kernels (lbm_step_q*.cu), so the library
+// builds in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "lbm_step.cuh"
+
+namespace lbm {
+
+struct Launch {
+   dim3 grid, block;
+   cudaStream_t stream;
+};
+
+template <int Q, int ST, int AR, int KIND>
+cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void* dst, bool links,
+                        bool fields)
+{
+   using T = typename Store<ST>::T;
+   const T* s = static_cast<const T*>(src);
+   T* d = static_cast<T*>(dst);
+   // Per-cell fields always use the exact FP64 arithmetic when FP64 is stored.
+   constexpr int ARF = (AR == AR_F64X) ? AR_F64 : AR;
+   if (links) {
+      if (fields) step_kernel<Q, ST, ARF, KIND, true, true><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+      else step_kernel<Q, ST, AR, KIND, true, false><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+   } else {
+      if (fields) step_kernel<Q, ST, ARF, KIND, false, true><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+      else step_kernel<Q, ST, AR, KIND, false, false><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+   }
+   return cudaGetLastError();
+}
+
+template <int Q, int ST, int AR>
+cudaError_t launch_step_t(int kind, const Launch& L, const KParams& p, const void* src, void* dst,
+                          bool links, bool fields)
+{
+   switch (kind) {
+      case K_AA_EVEN: return launch_kind<Q, ST, AR, K_AA_EVEN>(L, p, src, dst, links, fields);
+      case K_AA_ODD: return launch_kind<Q, ST, AR, K_AA_ODD>(L, p, src, dst, links, fields);
+      case K_AB_PUSH: return launch_kind<Q, ST, AR, K_AB_PUSH>(L, p, src, dst, links, fields);
+      default: return launch_kind<Q, ST, AR, K_AB_PULL>(L, p, src, dst, links, fields);
+   }
+}
+
+// Defined in lbm_step_q19_f64.cu, lbm_step_q19_low.cu, lbm_step_q27_f64.cu,
+// lbm_step_q27_low.cu.
+cudaError_t launch_step_q19_f64(int arith, int kind, const Launch& L, const KParams& p,
+                                const void* src, void* dst, bool links, bool fields);
+cudaError_t launch_step_q19_low(int storage, int kind, const Launch& L, const KParams& p,
+                                const void* src, void* dst, bool links, bool fields);
+cudaError_t launch_step_q27_f64(int arith, int kind, const Launch& L, const KParams& p,
+                                const void* src, void* dst, bool links, bool fields);
+cudaError_t launch_step_q27_low(int storage, int kind, const Launch& L, const KParams& p,
+                                const void* src, void* dst, bool links, bool fields);
+
+}  // namespace lbm

@@ -1,0 +1,189 @@
+// Collision arithmetic and population storage for the collide-stream kernels.
+//
+// The physics is the reference's BGK collision with Guo forcing
+// (src/kernels/KernelAA_SOA_Base.cpp:186-247):
+//   rho = sum f_s,  v = (sum c_s f_s + F/2) / rho
+//   eq_s    = w_s rho (1 + cu + cu^2/2 - uu/2),   cu = 3 c_s.v, uu = 3 v.v
+//   fdist_s = w_s (cf - fu + cu cf),              cf = 3 c_s.F, fu = 3 F.v
+//   f_s'    = (1-omega) f_s + omega eq_s + (1-omega/2) fdist_s
+// optionally followed by partial bounce-back with solid fraction sp:
+//   post_s  = (1-sp) f_s' + sp f_opp(s)
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <cstdint>
+
+#include "lbm_lattice.cuh"
+
+namespace lbm {
+
+enum StoreKind { ST_F64 = 0, ST_F32 = 1, ST_BF16 = 2, ST_F16 = 3 };
+enum ArithKind { AR_F64 = 1, AR_F64X = 2, AR_F32 = 3 };
+enum StepKind { K_AA_EVEN = 0, K_AA_ODD = 1, K_AB_PUSH = 2, K_AB_PULL = 3 };
+
+// Scale applied to shifted FP16 populations so that small deviations stay in
+// the normal range of binary16 (as in the FP16S format of Lehmann et al.
+// 2022, "Accuracy and performance of the lattice Boltzmann method with 64-bit,
+// 32-bit, and customized 16-bit number formats").
+constexpr float kF16Scale = 32768.0f;
+
+// Everything a step kernel needs, passed by value.
+struct KParams {
+   int nx, ny, nz;
+   int z0;               // first z plane covered by the launch
+   int64_t ncell;
+   int64_t plane;        // elements between direction planes
+   int64_t cstart, cend; // cell range handled by this launch
+   double omega, om1, om2;        // omega, 1-omega, 1-0.5*omega (as the reference folds them)
+   float omegaf, om1f, om2f;
+   double F[3];                   // uniform body force
+   float Ff[3];
+   int compat;                    // Q19 AA Unroll rest forcing weight
+   const uint32_t* links;         // per-cell link word or null
+   const double* force_field;     // planar [3][plane] (FP64 arithmetic) or null
+   const float* force_field_f;    // planar [3][plane] (FP32 arithmetic) or null
+   const double* porosity;        // [plane] or null
+   const float* porosity_f;
+   // Float-pair (hi, lo) splits of the launch constants for the F64X path,
+   // made on the host so no thread converts doubles.
+   float x_om1[2], x_omega[2];
+   float x_ow[4][2];              // omega * w per weight class (|c|^2 = 0..3)
+   float x_F[3][2];               // uniform force
+};
+
+// Link word: bit s set when the neighbour at x + c_s is solid or outside a
+// non-periodic face (half-way bounce-back); bit 31 set when x itself is solid.
+constexpr uint32_t kSolidBit = 0x80000000u;
+
+// ---------------------------------------------------------------- storage
+template <int ST> struct Store;
+template <> struct Store<ST_F64> { using T = double; static constexpr int bytes = 8; };
+template <> struct Store<ST_F32> { using T = float; static constexpr int bytes = 4; };
+template <> struct Store<ST_BF16> { using T = __nv_bfloat16; static constexpr int bytes = 2; };
+template <> struct Store<ST_F16> { using T = __half; static constexpr int bytes = 2; };
+
+// Shifted storage: the stored value is (f - w) (times kF16Scale for FP16).
+__device__ __forceinline__ float load_shifted(const float* p) { return *p; }
+__device__ __forceinline__ float load_shifted(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ float load_shifted(const __half* p)
+{
+   return __half2float(*p) * (1.0f / kF16Scale);
+}
+__device__ __forceinline__ void store_shifted(float* p, float g) { *p = g; }
+__device__ __forceinline__ void store_shifted(__nv_bfloat16* p, float g) { *p = __float2bfloat16_rn(g); }
+__device__ __forceinline__ void store_shifted(__half* p, float g) { *p = __float2half_rn(g * kF16Scale); }
+
+// ------------------------------------------------- exact FP64 collision
+// Operation order and association of KernelAA_SOA_Base.cpp:186-247 with every
+// operation an explicitly rounded IEEE double op (no FMA contraction), so the
+// result is bit-identical to the reference CPU build.  Terms whose stencil
+// component is zero are skipped: the reference adds d*0.0 = +-0.0, which
+// leaves every non-zero partial sum unchanged.
+template <int Q, int S>
+__device__ __forceinline__ double cdot_exact(double a0, double a1, double a2)
+{
+   constexpr int c0 = lat_c(Q, S, 0), c1 = lat_c(Q, S, 1), c2 = lat_c(Q, S, 2);
+   double acc = 0.0;
+   bool any = false;
+   if (c0 != 0) { acc = c0 > 0 ? a0 : -a0; any = true; }
+   if (c1 != 0) { acc = any ? (c1 > 0 ? __dadd_rn(acc, a1) : __dsub_rn(acc, a1)) : (c1 > 0 ? a1 : -a1); any = true; }
+   if (c2 != 0) { acc = any ? (c2 > 0 ? __dadd_rn(acc, a2) : __dsub_rn(acc, a2)) : (c2 > 0 ? a2 : -a2); any = true; }
+   return acc;
+}
+
+template <int Q, int S = 0>
+__device__ __forceinline__ void eq_update_exact(double (&d)[Q], double (&o)[Q], double rho, double v0,
+                                                double v1, double v2, double F0, double F1, double F2,
+                                                double vdotv, double fdotv, const KParams& p)
+{
+   if constexpr (S < Q) {
+      const double cdotv = __dmul_rn(3.0, cdot_exact<Q, S>(v0, v1, v2));
+      const double cdotf = __dmul_rn(3.0, cdot_exact<Q, S>(F0, F1, F2));
+      constexpr double w = lat_w(Q, S);
+      const double eq = __dmul_rn(
+         __dmul_rn(w, rho),
+         __dsub_rn(__dadd_rn(__dadd_rn(1.0, cdotv), __dmul_rn(__dmul_rn(0.5, cdotv), cdotv)),
+                   __dmul_rn(0.5, vdotv)));
+      const double wf = (Q == 19 && S == lat_rest(Q) && p.compat) ? 1.0 / 36.0 : w;
+      const double fdist = __dmul_rn(wf, __dadd_rn(__dsub_rn(cdotf, fdotv), __dmul_rn(cdotv, cdotf)));
+      o[S] = __dadd_rn(__dadd_rn(__dmul_rn(p.om1, d[S]), __dmul_rn(p.omega, eq)), __dmul_rn(p.om2, fdist));
+      eq_update_exact<Q, S + 1>(d, o, rho, v0, v1, v2, F0, F1, F2, vdotv, fdotv, p);
+   }
+}
+
+template <int Q>
+__device__ __forceinline__ void collide_f64(double (&d)[Q], double (&o)[Q], double F0, double F1,
+                                            double F2, double sp, const KParams& p)
+{
+   double rho = 0.0, v0 = 0.0, v1 = 0.0, v2 = 0.0;
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      rho = __dadd_rn(rho, d[s]);
+      const int c0 = lat_c(Q, s, 0), c1 = lat_c(Q, s, 1), c2 = lat_c(Q, s, 2);
+      if (c0 > 0) v0 = __dadd_rn(v0, d[s]); else if (c0 < 0) v0 = __dsub_rn(v0, d[s]);
+      if (c1 > 0) v1 = __dadd_rn(v1, d[s]); else if (c1 < 0) v1 = __dsub_rn(v1, d[s]);
+      if (c2 > 0) v2 = __dadd_rn(v2, d[s]); else if (c2 < 0) v2 = __dsub_rn(v2, d[s]);
+   }
+   v0 = __dadd_rn(v0, __dmul_rn(0.5, F0));
+   v1 = __dadd_rn(v1, __dmul_rn(0.5, F1));
+   v2 = __dadd_rn(v2, __dmul_rn(0.5, F2));
+   const double invRho = __ddiv_rn(1.0, rho);
+   v0 = __dmul_rn(v0, invRho);
+   v1 = __dmul_rn(v1, invRho);
+   v2 = __dmul_rn(v2, invRho);
+   const double vdotv =
+      __dmul_rn(3.0, __dadd_rn(__dadd_rn(__dmul_rn(v0, v0), __dmul_rn(v1, v1)), __dmul_rn(v2, v2)));
+   const double fdotv =
+      __dmul_rn(3.0, __dadd_rn(__dadd_rn(__dmul_rn(F0, v0), __dmul_rn(F1, v1)), __dmul_rn(F2, v2)));
+   eq_update_exact<Q>(d, o, rho, v0, v1, v2, F0, F1, F2, vdotv, fdotv, p);
+   if (sp != 0.0) {
+      const double keep = __dsub_rn(1.0, sp);
+#pragma unroll
+      for (int s = 0; s < Q; s++) o[s] = __dadd_rn(__dmul_rn(keep, o[s]), __dmul_rn(sp, d[lat_opp(Q, s)]));
+   }
+}
+
+// ------------------------------------------- FP32 shifted collision
+// g = f - w.  With drho = sum g (sum w = 1) and j = sum c g (sum c w = 0):
+//   eq_s - w_s = w_s (drho + rho (cu + cu^2/2 - uu/2))
+//   g_s'       = (1-omega) g_s + omega (eq_s - w_s) + (1-omega/2) fdist_s
+// which keeps the large constant w out of the single-precision arithmetic.
+template <int Q>
+__device__ __forceinline__ void collide_f32(float (&g)[Q], float (&o)[Q], float F0, float F1, float F2,
+                                            float sp, const KParams& p)
+{
+   float drho = 0.f, j0 = 0.f, j1 = 0.f, j2 = 0.f;
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      drho += g[s];
+      const int c0 = lat_c(Q, s, 0), c1 = lat_c(Q, s, 1), c2 = lat_c(Q, s, 2);
+      if (c0 > 0) j0 += g[s]; else if (c0 < 0) j0 -= g[s];
+      if (c1 > 0) j1 += g[s]; else if (c1 < 0) j1 -= g[s];
+      if (c2 > 0) j2 += g[s]; else if (c2 < 0) j2 -= g[s];
+   }
+   const float rho = 1.0f + drho;
+   const float ir = __frcp_rn(rho);
+   const float u0 = (j0 + 0.5f * F0) * ir, u1 = (j1 + 0.5f * F1) * ir, u2 = (j2 + 0.5f * F2) * ir;
+   const float uu = 3.0f * (u0 * u0 + u1 * u1 + u2 * u2);
+   const float fu = 3.0f * (F0 * u0 + F1 * u1 + F2 * u2);
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      const float c0 = (float)lat_c(Q, s, 0), c1 = (float)lat_c(Q, s, 1), c2 = (float)lat_c(Q, s, 2);
+      const float cu = 3.0f * (c0 * u0 + c1 * u1 + c2 * u2);
+      const float cf = 3.0f * (c0 * F0 + c1 * F1 + c2 * F2);
+      const float w = (float)lat_w(Q, s);
+      const float wf = (Q == 19 && s == lat_rest(Q) && p.compat) ? (float)(1.0 / 36.0) : w;
+      const float eqm = w * (drho + rho * (cu + 0.5f * cu * cu - 0.5f * uu));
+      const float fd = wf * (cf - fu + cu * cf);
+      o[s] = p.om1f * g[s] + p.omegaf * eqm + p.om2f * fd;
+   }
+   if (sp != 0.0f) {
+      const float keep = 1.0f - sp;
+#pragma unroll
+      for (int s = 0; s < Q; s++) o[s] = keep * o[s] + sp * g[lat_opp(Q, s)];
+   }
+}
+
+}  // namespace lbm

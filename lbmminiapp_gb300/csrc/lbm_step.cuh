@@ -1,0 +1,165 @@
+// Fused collide-stream step kernels.
+//
+// One thread per cell along the contiguous x axis; a 3-D grid
+// (x blocks, y, z) so no per-thread division is needed.  Population buffers
+// are planar: direction s of cell c lives at s*plane + c.
+//
+// Streaming replaces the reference's int32 adjacency list
+// (src/geometries/GeometryAAAB.cpp:18-124) with index arithmetic: the
+// neighbour x +- c_s wraps on periodic axes, and a per-cell 32-bit link word
+// (present only when the geometry has solids or non-periodic faces) says
+// which neighbours bounce back to the own cell's opposite slot.
+//
+//   AA even  (KernelAA_SOA_Base.cpp:173-254): read own slot opp(s), write own slot s
+//   AA odd   (KernelAA_SOA_Base.cpp:257-342): read slot s at x - c_s (or own slot opp(s)),
+//            write slot opp(s) at x + c_s (or own slot s)
+//   AB push  (KernelAB_SOA_Base.cpp:111-186): read own slot s from src, write slot s at
+//            x + c_s (or own slot opp(s)) in tgt
+//   AB pull  (KernelAB_SOA_Pull.cpp:113-194): read slot s at x - c_s (or own slot opp(s))
+//            from src, write own slot s in tgt
+#pragma once
+
+#include "lbm_f64x.cuh"
+#include "lbm_physics.cuh"
+
+namespace lbm {
+
+struct CellIndex {
+   int64_t c;
+   int dxm, dxp, dym, dyp;   // neighbour offsets in cells along x and y
+   int64_t dzm, dzp;
+};
+
+__device__ __forceinline__ bool cell_of_thread(const KParams& p, CellIndex& ci)
+{
+   const int x = blockIdx.x * blockDim.x + threadIdx.x;
+   const int y = blockIdx.y;
+   const int z = p.z0 + blockIdx.z;
+   if (x >= p.nx) return false;
+   const int64_t row = (int64_t)z * p.ny + y;
+   ci.c = row * p.nx + x;
+   if (ci.c < p.cstart || ci.c >= p.cend) return false;
+   ci.dxm = (x == 0) ? p.nx - 1 : -1;
+   ci.dxp = (x == p.nx - 1) ? -(p.nx - 1) : 1;
+   ci.dym = (y == 0) ? (p.ny - 1) * p.nx : -p.nx;
+   ci.dyp = (y == p.ny - 1) ? -(p.ny - 1) * p.nx : p.nx;
+   const int64_t nxy = (int64_t)p.nx * p.ny;
+   ci.dzm = (z == 0) ? (int64_t)(p.nz - 1) * nxy : -nxy;
+   ci.dzp = (z == p.nz - 1) ? -(int64_t)(p.nz - 1) * nxy : nxy;
+   return true;
+}
+
+// Cell index of x + (sx, sy, sz) with periodic wrap on every axis (a wrapped
+// neighbour across a non-periodic face is always flagged in the link word and
+// never dereferenced).
+__device__ __forceinline__ int64_t nbr(const CellIndex& ci, int sx, int sy, int sz)
+{
+   int64_t n = ci.c;
+   if (sx > 0) n += ci.dxp; else if (sx < 0) n += ci.dxm;
+   if (sy > 0) n += ci.dyp; else if (sy < 0) n += ci.dym;
+   if (sz > 0) n += ci.dzp; else if (sz < 0) n += ci.dzm;
+   return n;
+}
+
+// Source (slot index) that direction s of this cell is read from.
+template <int Q, int KIND, bool LINKS>
+__device__ __forceinline__ int64_t read_index(const KParams& p, const CellIndex& ci, uint32_t lk, int s)
+{
+   const int o = lat_opp(Q, s);
+   if (KIND == K_AA_EVEN) return (int64_t)o * p.plane + ci.c;
+   if (KIND == K_AB_PUSH || s == lat_rest(Q)) return (int64_t)s * p.plane + ci.c;
+   // AA odd, AB pull: slot s at x - c_s unless that neighbour is blocked.
+   if (LINKS && ((lk >> o) & 1u)) return (int64_t)o * p.plane + ci.c;
+   return (int64_t)s * p.plane + nbr(ci, -lat_c(Q, s, 0), -lat_c(Q, s, 1), -lat_c(Q, s, 2));
+}
+
+// Destination (slot index) of the post-collision value of direction s.
+template <int Q, int KIND, bool LINKS>
+__device__ __forceinline__ int64_t write_index(const KParams& p, const CellIndex& ci, uint32_t lk, int s)
+{
+   const int o = lat_opp(Q, s);
+   if (KIND == K_AA_EVEN || KIND == K_AB_PULL || s == lat_rest(Q)) return (int64_t)s * p.plane + ci.c;
+   const bool blocked = LINKS && ((lk >> s) & 1u);
+   if (KIND == K_AA_ODD) {
+      if (blocked) return (int64_t)s * p.plane + ci.c;
+      return (int64_t)o * p.plane + nbr(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+   }
+   // AB push
+   if (blocked) return (int64_t)o * p.plane + ci.c;
+   return (int64_t)s * p.plane + nbr(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+}
+
+template <bool FIELDS>
+__device__ __forceinline__ void cell_force_f64(const KParams& p, int64_t c, double& F0, double& F1,
+                                               double& F2, double& sp)
+{
+   F0 = p.F[0]; F1 = p.F[1]; F2 = p.F[2]; sp = 0.0;
+   if (FIELDS) {
+      if (p.force_field) {
+         F0 = __dadd_rn(F0, p.force_field[c]);
+         F1 = __dadd_rn(F1, p.force_field[p.plane + c]);
+         F2 = __dadd_rn(F2, p.force_field[2 * p.plane + c]);
+      }
+      if (p.porosity) sp = p.porosity[c];
+   }
+}
+
+template <bool FIELDS>
+__device__ __forceinline__ void cell_force_f32(const KParams& p, int64_t c, float& F0, float& F1,
+                                               float& F2, float& sp)
+{
+   F0 = p.Ff[0]; F1 = p.Ff[1]; F2 = p.Ff[2]; sp = 0.0f;
+   if (FIELDS) {
+      if (p.force_field_f) {
+         F0 += p.force_field_f[c];
+         F1 += p.force_field_f[p.plane + c];
+         F2 += p.force_field_f[2 * p.plane + c];
+      }
+      if (p.porosity_f) sp = p.porosity_f[c];
+   }
+}
+
+// One launch = one time step (or one range of it) of one propagation kind.
+template <int Q, int ST, int AR, int KIND, bool LINKS, bool FIELDS>
+__global__ void __launch_bounds__(256) step_kernel(const KParams p, const typename Store<ST>::T* src,
+                                                   typename Store<ST>::T* dst)
+{
+   CellIndex ci;
+   if (!cell_of_thread(p, ci)) return;
+   uint32_t lk = 0;
+   if (LINKS) {
+      lk = p.links[ci.c];
+      if (lk & kSolidBit) return;
+   }
+   if constexpr (AR == AR_F64) {
+      double d[Q], o[Q];
+#pragma unroll
+      for (int s = 0; s < Q; s++) d[s] = src[read_index<Q, KIND, LINKS>(p, ci, lk, s)];
+      double F0, F1, F2, sp;
+      cell_force_f64<FIELDS>(p, ci.c, F0, F1, F2, sp);
+      collide_f64<Q>(d, o, F0, F1, F2, sp, p);
+#pragma unroll
+      for (int s = 0; s < Q; s++) dst[write_index<Q, KIND, LINKS>(p, ci, lk, s)] = o[s];
+   } else if constexpr (AR == AR_F64X) {
+      uint64_t bits[Q];
+      const unsigned long long* s64 = reinterpret_cast<const unsigned long long*>(src);
+#pragma unroll
+      for (int s = 0; s < Q; s++) bits[s] = s64[read_index<Q, KIND, LINKS>(p, ci, lk, s)];
+      static_assert(!FIELDS, "per-cell fields use the exact FP64 arithmetic");
+      collide_f64x<Q>(bits, p);
+      unsigned long long* d64 = reinterpret_cast<unsigned long long*>(dst);
+#pragma unroll
+      for (int s = 0; s < Q; s++) d64[write_index<Q, KIND, LINKS>(p, ci, lk, s)] = bits[s];
+   } else {
+      float g[Q], o[Q];
+#pragma unroll
+      for (int s = 0; s < Q; s++) g[s] = load_shifted(src + read_index<Q, KIND, LINKS>(p, ci, lk, s));
+      float F0, F1, F2, sp;
+      cell_force_f32<FIELDS>(p, ci.c, F0, F1, F2, sp);
+      collide_f32<Q>(g, o, F0, F1, F2, sp, p);
+#pragma unroll
+      for (int s = 0; s < Q; s++) store_shifted(dst + write_index<Q, KIND, LINKS>(p, ci, lk, s), o[s]);
+   }
+}
+
+}  // namespace lbm

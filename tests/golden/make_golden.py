@@ -1,0 +1,65 @@
+"""Generate the golden fixtures in this directory from the reference itself.
+
+Runs the UNMODIFIED lbmminiapp CPU kernels (compiled by oracle/build_ref.sh,
+driven by oracle/ref_harness.cpp) on small seeded cases and stores inputs and
+final raw population buffers as .npz files.  The reference sources are needed
+only to regenerate; the fixtures themselves are committed so parity checks run
+where the reference is absent.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[1]))
+
+from oracle import core, ref  # noqa: E402
+from lbmminiapp_gb300 import workloads  # noqa: E402
+
+# name: (Q, variant, pattern, compat, (nx, ny, nz), periodic, walls, tau, gx, steps, U, noise)
+CASES = {
+    "q19_aa_base_tg_box": (19, ref.AA_BASE, core.AA, 0, (12, 10, 8), (1, 1, 1), False, 0.8, 0.0, 20, 0.05, 0.0),
+    "q19_aa_unroll_channel_force": (19, ref.AA_UNROLL, core.AA, 1, (10, 9, 6), (1, 0, 1), True, 0.6, 1e-5, 15,
+                                    0.02, 1e-3),
+    "q19_ab_push_unroll_channel": (19, ref.AB_PUSH_UNROLL, core.AB_PUSH, 0, (9, 8, 7), (1, 0, 1), True, 0.7, 1e-5,
+                                   11, 0.02, 1e-3),
+    "q19_ab_pull_base_odd_box": (19, ref.AB_PULL_BASE, core.AB_PULL, 0, (17, 9, 5), (1, 1, 1), False, 0.55, 1e-6,
+                                 9, 0.05, 1e-3),
+    "q27_aa_base_tg_box": (27, ref.AA_BASE, core.AA, 0, (8, 8, 8), (1, 1, 1), False, 0.8, 0.0, 13, 0.05, 0.0),
+    "q27_ab_push_channel_force": (27, ref.AB_PUSH_BASE, core.AB_PUSH, 0, (10, 8, 6), (1, 0, 1), True, 0.6, 1e-6,
+                                  12, 0.0, 0.0),
+    "q27_ab_pull_channel_force": (27, ref.AB_PULL_BASE, core.AB_PULL, 0, (10, 8, 6), (1, 0, 1), True, 0.6, 1e-6,
+                                  12, 0.0, 0.0),
+}
+
+
+def case_inputs(Q, dims, walls, U, noise, seed=7):
+    nx, ny, nz = dims
+    u = workloads.taylor_green(nx, ny, nz, U=U, noise=noise, seed=seed)
+    rho = 1.0 + workloads.uniform_noise((nz, ny, nx), seed, 3, 1e-3 if noise else 0.0)
+    solid = workloads.channel_mask(nx, ny, nz) if walls else np.zeros((nz, ny, nx), np.uint8)
+    if walls:
+        u[:, solid.astype(bool)] = 0.0
+    f0 = core.equilibrium(Q, rho, u)
+    return f0, solid
+
+
+def main():
+    if not ref.available():
+        sys.exit("reference harness unavailable (oracle/build_ref.sh needs the reference sources)")
+    for name, (Q, variant, pattern, compat, dims, per, walls, tau, gx, steps, U, noise) in CASES.items():
+        f0, solid = case_inputs(Q, dims, walls, U, noise)
+        raw, _ = ref.box_run(Q, variant, f0, steps, 1.0 / tau, gx, per, solid)
+        np.savez_compressed(HERE / f"{name}.npz", Q=Q, pattern=pattern, compat=compat, dims=np.array(dims),
+                            periodic=np.array(per), solid=solid, omega=1.0 / tau, gx=gx, steps=steps,
+                            f_init=f0, f_raw=raw, variant=variant)
+        print(f"{name}: {raw.nbytes + f0.nbytes} bytes")
+
+
+if __name__ == "__main__":
+    main()
