@@ -1,0 +1,341 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 collide-stream path (one JSON line on stdout).
+
+Workload (the headline configuration): D3Q19 BGK + Guo, AA propagation, SOA,
+512^3 fully periodic box, tau = 0.55, Taylor-Green vortex (peak 0.05) plus
+seeded uniform +-1e-3 velocity noise, FP64 population storage.  One bench step
+is one lattice time step over the whole box (one kernel launch); the state is
+20.4 GB, far larger than the 129 MB L2, so no flush is needed between steps.
+
+* value      MLUPS with the state resident in HBM, CUDA events on the launch
+             stream, max over ranks (independent replicas when --gpus > 1);
+* e2e        the same metric through the C ABI from pinned host memory: the
+             initial velocity field is copied in, 100 steps run and rho/u are
+             copied back, all inside the timed region;
+* roofline   HBM bound: algorithmic bytes 2*Q*8 = 304 B per fluid-cell update
+             over the measured copy bandwidth (MEASURED_PEAKS.json);
+* cpu_baseline  the oracle port (C restatement of the reference's CPU kernels,
+             OpenMP on all host cores) on a bounded sample of the workload.
+
+``--impl reference`` times that CPU implementation alone (each step one lattice
+step of a 256^3 sample of the same workload) and prints the same line shape.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MLUPS (D3Q19 AA FP64, 512^3 Taylor-Green box)"
+UNIT = "MLUPS"
+TAU = 0.55
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=512, help="box edge (cells)")
+    ap.add_argument("--no-variants", action="store_true", help="skip the other storage formats")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend)
+        return dist, rank, world, local
+    return None, rank, world, local
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload_velocity(n, seed=2024):
+    from lbmminiapp_gb300 import workloads
+    return workloads.taylor_green(n, n, n, U=0.05, noise=1e-3, seed=seed)
+
+
+def cpu_port_mlups(n, target_seconds=10.0, nthreads=0):
+    """Oracle port (C restatement, OpenMP) on an n^3 sample of the workload:
+    returns (MLUPS, threads, steps, seconds)."""
+    from oracle import core
+    u = workload_velocity(n)
+    f0 = core.equilibrium(19, np.ones((n, n, n)), u)
+    del u
+    runner = core.Runner(19, core.AA, f0, 1.0 / TAU, nthreads=nthreads)
+    del f0
+    runner.step(2)
+    t = runner.step(2)
+    steps = max(2, int(target_seconds / max(t / 2, 1e-6)) // 2 * 2)
+    t = runner.step(steps)
+    threads = nthreads if nthreads > 0 else core.max_threads()
+    runner.close()
+    return n ** 3 * steps / t / 1e6, threads, steps, t
+
+
+def traffic_per_launch():
+    """DRAM bytes per step launch from the committed ncu summary, scaled to a
+    512^3 launch (null when no capture is committed)."""
+    p = ROOT / "profiles" / "aa_step_f64x_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    return d.get("bytes_per_launch_512")
+
+
+def run_reference_arm(args, dist, rank, world):
+    if rank != 0:
+        return 0
+    from oracle import core
+    n = 256
+    u = workload_velocity(n)
+    f0 = core.equilibrium(19, np.ones((n, n, n)), u)
+    del u
+    runner = core.Runner(19, core.AA, f0, 1.0 / TAU)
+    del f0
+    threads = core.max_threads()
+    for _ in range(args.warmup):
+        runner.step(1)
+    times = [runner.step(1) for _ in range(args.steps)]
+    runner.close()
+    total = sum(times)
+    mlups = n ** 3 * args.steps / total / 1e6
+    line = {
+        "metric": METRIC, "value": round(mlups, 3), "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Taylor-Green + SplitMix64 noise)",
+        "config": {"workload": "D3Q19 AA FP64 Taylor-Green periodic box, tau=0.55; each step one lattice "
+                               "step of a 256^3 sample (1/8 of the 512^3 box)", "lattice": "D3Q19",
+                   "propagation": "AA", "grid": [n, n, n], "storage": "f64"},
+        "cpu_baseline": {"value": round(mlups, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n}^3 box, {args.steps} timed lattice steps; oracle/lbm_oracle.c "
+                                   "(C restatement of the reference's AA kernels, int32 adjacency, OpenMP)"},
+        "e2e": {"value": round(mlups, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    dist, rank, world, local = dist_setup(args)
+    if args.impl == "reference":
+        return run_reference_arm(args, dist, rank, world)
+
+    import torch
+    import lbmminiapp_gb300 as lbm
+
+    torch.cuda.set_device(local)
+    n = args.n
+    ncell = n ** 3
+    Q = 19
+    bpu = 2 * Q * 8
+    u = workload_velocity(n)
+    sim = lbm.Simulation(n, n, n, lattice=Q, pattern="aa", omega=1.0 / TAU, force=(0, 0, 0), storage="f64",
+                         arithmetic="f64x", device=local)
+    sim.init_equilibrium(None, u)
+    for _ in range(max(args.warmup, 3)):
+        sim.step(1)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        ev[0].record()
+        for k in range(args.steps):
+            sim.step(1)
+            ev[k + 1].record()
+        ev[-1].synchronize()
+    torch.cuda.synchronize()
+    per_launch_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+        dist.barrier()
+    value = world * ncell * args.steps / (total_ms * 1e-3) / 1e6
+    mass = float(sim.conserved()[0]) / ncell
+    launches = args.steps
+
+    peak, peak_kind = measured_peaks()
+    avg_launch_s = statistics.mean(per_launch_ms) * 1e-3
+    achieved = ncell * bpu / avg_launch_s / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic_per_launch(),
+                "peak_kind": f"{peak_kind} copy bandwidth",
+                "kernel": "step_kernel<19,F64,F64X,AA_EVEN|AA_ODD> (one launch per step)",
+                "algorithmic_bytes_per_launch": ncell * bpu}
+
+    # end to end through the C ABI, pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        steps_e2e = 100
+        u_host = torch.empty((3, n, n, n), dtype=torch.float64, pin_memory=True)
+        u_host.numpy()[...] = u
+        rho_out = torch.empty((n, n, n), dtype=torch.float64, pin_memory=True)
+        u_out = torch.empty((3, n, n, n), dtype=torch.float64, pin_memory=True)
+        times = []
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sim.init_equilibrium(None, u_host.numpy())
+            sim.step(steps_e2e)
+            sim.macros(out=(rho_out.numpy(), u_out.numpy()))
+            times.append(time.perf_counter() - t0)
+        launches_e2e = steps_e2e + 2
+        e2e = {"value": round(ncell * steps_e2e / times[-1] / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": 3 * 8 * ncell, "d2h_bytes_per_step": 4 * 8 * ncell,
+               "step": f"init_equilibrium(u from pinned host) + {steps_e2e} lattice steps + get_macros "
+                       "(rho, u to pinned host)",
+               "gpu_launches_per_step": launches_e2e}
+        del u_host, rho_out, u_out
+    sim.close()
+    del u
+
+    variants = {}
+    if not args.no_variants:
+        uv = workload_velocity(n)
+        for storage, arith, steps in [("f16", "auto", 12), ("bf16", "auto", 12), ("f32", "auto", 12),
+                                      ("f64", "f64", 3)]:
+            s2 = lbm.Simulation(n, n, n, lattice=Q, pattern="aa", omega=1.0 / TAU, force=(0, 0, 0),
+                                storage=storage, arithmetic=arith, device=local)
+            s2.init_equilibrium(None, uv)
+            s2.step(2)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            s2.step(steps)
+            b.record()
+            b.synchronize()
+            ms = a.elapsed_time(b) / steps
+            bytes_u = s2.info.bytes_per_update
+            variants[f"{storage}/{arith}"] = {"MLUPS": round(ncell / (ms * 1e-3) / 1e6, 1),
+                                              "GB/s": round(ncell * bytes_u / (ms * 1e-3) / 1e9, 1),
+                                              "bytes_per_update": bytes_u}
+            s2.close()
+        del uv
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        sample_n = 128
+        mlups_cpu, threads, csteps, csec = cpu_port_mlups(sample_n)
+        cpu = {"value": round(mlups_cpu, 3), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{sample_n}^3 box of the same workload, {csteps} lattice steps in {csec:.1f} s; "
+                         "oracle/lbm_oracle.c (C restatement of the reference AA kernels, int32 adjacency, "
+                         "OpenMP)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(total_ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 storage, df64 (FP32-pair) arithmetic",
+            "data": "synthetic (seeded Taylor-Green + SplitMix64 noise)",
+            "config": {"workload": "D3Q19 BGK AA, 512^3 periodic box, tau=0.55, Taylor-Green U=0.05 + "
+                                   "uniform 1e-3 noise, FP64 storage",
+                       "lattice": "D3Q19", "propagation": "AA", "grid": [n, n, n], "tau": TAU,
+                       "storage": "f64", "arithmetic": "F64X (within 1e-10 of the reference)",
+                       "l2": "state 20.4 GB >> 129 MB L2 (no flush needed)",
+                       "parallelism": "independent replica per GPU" if world > 1 else "1 GPU"},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "variants": variants,
+            "mass_per_cell_after": mass,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -131,9 +131,17 @@ class Simulation:
     def step(self, n=1):
         self._check(self.lib.lbm_step(self.h, int(n)))
 
-    def macros(self):
-        rho = np.empty(self.shape)
-        u = np.empty((3,) + self.shape)
+    def macros(self, out=None):
+        """(rho, u) with the reference readout semantics; ``out`` may supply
+        preallocated (rho, u) float64 arrays (e.g. views of pinned memory)."""
+        if out is None:
+            rho = np.empty(self.shape)
+            u = np.empty((3,) + self.shape)
+        else:
+            rho, u = out
+            assert rho.shape == self.shape and u.shape == (3,) + self.shape
+            assert rho.dtype == np.float64 and u.dtype == np.float64
+            assert rho.flags.c_contiguous and u.flags.c_contiguous
         self._check(self.lib.lbm_get_macros(self.h, N.ptr(rho), N.ptr(u)))
         return rho, u
 

@@ -82,6 +82,13 @@ def lib():
                                                                               ctypes.c_int, P, P]
         L.lbm_oracle_run.restype = ctypes.c_int
         L.lbm_oracle_max_threads.restype = ctypes.c_int
+        L.lbm_oracle_create.argtypes = [ctypes.c_int] * 6 + [P, P, ctypes.c_double, P, P, P, P, ctypes.c_int]
+        L.lbm_oracle_create.restype = ctypes.c_void_p
+        L.lbm_oracle_step.argtypes = [P, ctypes.c_int, P]
+        L.lbm_oracle_read.argtypes = [P, P]
+        L.lbm_oracle_destroy.argtypes = [P]
+        L.lbm_oracle_fluid_count.argtypes = [P]
+        L.lbm_oracle_fluid_count.restype = ctypes.c_longlong
         _lib = L
     return _lib
 
@@ -110,6 +117,50 @@ def run(Q, pattern, f_init, nsteps, omega, force=(0.0, 0.0, 0.0), periodic=(1, 1
     if rc:
         raise RuntimeError(f"lbm_oracle_run failed with code {rc}")
     return out, sec.value
+
+
+class Runner:
+    """Persistent oracle state for timing individual steps (CPU baseline)."""
+
+    def __init__(self, Q, pattern, f_init, omega, force=(0.0, 0.0, 0.0), periodic=(1, 1, 1), solid=None,
+                 compat_rest_weight=False, nthreads=0):
+        self._keep = [np.ascontiguousarray(periodic, dtype=np.int32),
+                      None if solid is None else np.ascontiguousarray(solid, dtype=np.uint8),
+                      np.ascontiguousarray(force, dtype=np.float64),
+                      np.ascontiguousarray(f_init, dtype=np.float64)]
+        per, sol, frc, f0 = self._keep
+        _, nz, ny, nx = f0.shape
+        self.Q = Q
+        self.shape = (nz, ny, nx)
+        self.h = lib().lbm_oracle_create(Q, pattern, int(bool(compat_rest_weight)), nx, ny, nz, _ptr(per),
+                                         _ptr(sol), float(omega), _ptr(frc), None, None, _ptr(f0),
+                                         int(nthreads))
+        if not self.h:
+            raise RuntimeError("lbm_oracle_create failed")
+        self._keep[3] = None  # initial populations were copied
+
+    @property
+    def nfluid(self) -> int:
+        return int(lib().lbm_oracle_fluid_count(self.h))
+
+    def step(self, n=1) -> float:
+        sec = ctypes.c_double(0.0)
+        if lib().lbm_oracle_step(self.h, int(n), ctypes.byref(sec)):
+            raise RuntimeError("lbm_oracle_step failed")
+        return sec.value
+
+    def read(self):
+        out = np.empty((self.Q,) + self.shape)
+        lib().lbm_oracle_read(self.h, _ptr(out))
+        return out
+
+    def close(self):
+        if self.h:
+            lib().lbm_oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
 
 
 def max_threads() -> int:

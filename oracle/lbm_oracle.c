@@ -130,7 +130,8 @@ typedef struct {
    int pattern; /* 0 AA, 1 AB push, 2 AB pull */
    int64_t nFluid;
    int64_t* fluidCell; /* dense cell index of each fluid point */
-   int64_t* adj;       /* [Q][nFluid] slot indices */
+   int64_t* adj;       /* [Q][nFluid] slot indices (used when adj32 is NULL) */
+   int32_t* adj32;     /* the same as int32, as the reference stores it, when Q*nFluid < 2^31 */
    double omega;
    double force[3];
    const double* forceField; /* planar [3][ncell] or NULL */
@@ -179,8 +180,17 @@ static int build_state(oracle_state* S, int Q, int pattern, int compat, int nx, 
       }
    }
    free(fluidIdx);
+   if ((int64_t)Q * nf < 2147483647LL) {
+      S->adj32 = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nf > 0 ? nf : 1) * Q);
+      if (!S->adj32) return 2;
+      for (int64_t k = 0; k < (int64_t)Q * nf; k++) S->adj32[k] = (int32_t)S->adj[k];
+      free(S->adj);
+      S->adj = NULL;
+   }
    return 0;
 }
+
+#define ADJ(S, k) ((S)->adj32 ? (int64_t)(S)->adj32[k] : (S)->adj[k])
 
 static inline void cell_params(const oracle_state* S, int64_t i, double* F, double* sp)
 {
@@ -223,7 +233,7 @@ static void aa_odd(const oracle_state* S, double* f)
       int64_t loc[ORACLE_MAXQ];
       cell_params(S, i, F, &sp);
       for (int s = 0; s < Q; s++) {
-         loc[s] = S->adj[(int64_t)s * nf + i];
+         loc[s] = ADJ(S, (int64_t)s * nf + i);
          d[s] = f[loc[s]];
       }
       collide_cell(&S->L, d, o, S->omega, F, sp);
@@ -243,7 +253,7 @@ static void ab_push(const oracle_state* S, const double* src, double* tgt)
       cell_params(S, i, F, &sp);
       for (int s = 0; s < Q; s++) d[s] = src[(int64_t)s * nf + i];
       collide_cell(&S->L, d, o, S->omega, F, sp);
-      for (int s = 0; s < Q; s++) tgt[S->adj[(int64_t)s * nf + i]] = o[s];
+      for (int s = 0; s < Q; s++) tgt[ADJ(S, (int64_t)s * nf + i)] = o[s];
    }
 }
 
@@ -257,7 +267,7 @@ static void ab_pull(const oracle_state* S, const double* src, double* tgt)
    for (int64_t i = 0; i < nf; i++) {
       double d[ORACLE_MAXQ], o[ORACLE_MAXQ], F[3], sp;
       cell_params(S, i, F, &sp);
-      for (int s = 0; s < Q; s++) d[s] = src[S->adj[(int64_t)s * nf + i]];
+      for (int s = 0; s < Q; s++) d[s] = src[ADJ(S, (int64_t)s * nf + i)];
       collide_cell(&S->L, d, o, S->omega, F, sp);
       for (int s = 0; s < Q; s++) tgt[(int64_t)s * nf + i] = o[s];
    }
@@ -279,87 +289,145 @@ int lbm_oracle_max_threads(void)
 #endif
 }
 
+typedef struct {
+   oracle_state S;
+   double* a;
+   double* b;
+   int64_t t;
+   int cur; /* AB: 0 -> a holds the latest state, 1 -> b */
+} oracle_run_state;
+
+void lbm_oracle_destroy(void* handle)
+{
+   oracle_run_state* R = (oracle_run_state*)handle;
+   if (!R) return;
+   free(R->a);
+   free(R->b);
+   free(R->S.fluidCell);
+   free(R->S.adj);
+   free(R->S.adj32);
+   free(R);
+}
+
 /*
- * Run nsteps of the collide-stream path and return the raw slot buffer the
- * reference would read back (AA: the single buffer; AB: the buffer holding
- * the latest step, i.e. dstrb_ after the swap in
- * src/propagation/PropagationAB.cpp:182-188).
- *
+ * Build the fluid list and adjacency and place the initial populations.
  * Q: 19 | 27.  pattern: 0 AA, 1 AB push, 2 AB pull.
  * f_init: logical populations (direction s of each cell), planar [Q][ncell];
  *         placed as the reference's initialize() places them: AA in slot
  *         opp(s) (PropagationAA.cpp:104-116), AB in slot s of both buffers
- *         (PropagationAB.cpp:130-143).
- * f_raw : out, planar [Q][ncell], NaN at solid cells.
- * nthreads <= 0 uses the OpenMP default.  seconds: wall time of the time loop.
- * Returns 0 on success, 1 for bad arguments, 2 for allocation failure.
+ *         (PropagationAB.cpp:130-143).  force_field / porosity must outlive
+ *         the handle.  nthreads <= 0 keeps the OpenMP default.
+ * Returns NULL on bad arguments or allocation failure.
  */
+void* lbm_oracle_create(int Q, int pattern, int compat_rest_weight, int nx, int ny, int nz,
+                        const int* periodic, const unsigned char* solid, double omega,
+                        const double* force, const double* force_field, const double* porosity,
+                        const double* f_init, int nthreads)
+{
+   if (nx <= 0 || ny <= 0 || nz <= 0 || pattern < 0 || pattern > 2) return NULL;
+#ifdef _OPENMP
+   if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+   (void)nthreads;
+#endif
+   oracle_run_state* R = (oracle_run_state*)calloc(1, sizeof(oracle_run_state));
+   if (!R) return NULL;
+   oracle_state* S = &R->S;
+   if (build_state(S, Q, pattern, compat_rest_weight, nx, ny, nz, periodic, solid)) {
+      lbm_oracle_destroy(R);
+      return NULL;
+   }
+   S->omega = omega;
+   for (int d = 0; d < 3; d++) S->force[d] = force ? force[d] : 0.0;
+   S->forceField = force_field;
+   S->porosity = porosity;
+   const int64_t nf = S->nFluid;
+   const int64_t ncell = S->ncell;
+   R->a = (double*)malloc(sizeof(double) * (size_t)(nf > 0 ? nf : 1) * Q);
+   R->b = (double*)malloc(sizeof(double) * (size_t)(nf > 0 ? nf : 1) * Q);
+   if (!R->a || !R->b) {
+      lbm_oracle_destroy(R);
+      return NULL;
+   }
+#pragma omp parallel for schedule(static)
+   for (int64_t i = 0; i < nf; i++) {
+      int64_t c = S->fluidCell[i];
+      for (int s = 0; s < Q; s++) {
+         double v = f_init[(int64_t)s * ncell + c];
+         if (pattern == 0) {
+            R->a[(int64_t)S->L.opp[s] * nf + i] = v;
+         } else {
+            R->a[(int64_t)s * nf + i] = v;
+            R->b[(int64_t)s * nf + i] = v;
+         }
+      }
+   }
+   return R;
+}
+
+/* Advance nsteps; seconds = wall time of the loop. */
+int lbm_oracle_step(void* handle, int nsteps, double* seconds)
+{
+   oracle_run_state* R = (oracle_run_state*)handle;
+   if (!R || nsteps < 0) return 1;
+   double t0 = now_seconds();
+   for (int k = 0; k < nsteps; k++) {
+      if (R->S.pattern == 0) {
+         if (R->t % 2 == 0) aa_even(&R->S, R->a);
+         else aa_odd(&R->S, R->a);
+      } else {
+         double* src = R->cur ? R->b : R->a;
+         double* tgt = R->cur ? R->a : R->b;
+         if (R->S.pattern == 1) ab_push(&R->S, src, tgt);
+         else ab_pull(&R->S, src, tgt);
+         R->cur = 1 - R->cur;
+      }
+      R->t++;
+   }
+   if (seconds) *seconds = now_seconds() - t0;
+   return 0;
+}
+
+long long lbm_oracle_fluid_count(void* handle)
+{
+   oracle_run_state* R = (oracle_run_state*)handle;
+   return R ? (long long)R->S.nFluid : -1;
+}
+
+/* Raw slot buffer the reference would read back (AA: the single buffer; AB:
+ * the buffer holding the latest step, i.e. dstrb_ after the swap in
+ * src/propagation/PropagationAB.cpp:182-188), planar [Q][ncell], NaN at solid
+ * cells. */
+int lbm_oracle_read(void* handle, double* f_raw)
+{
+   oracle_run_state* R = (oracle_run_state*)handle;
+   if (!R || !f_raw) return 1;
+   const int Q = R->S.L.Q;
+   const int64_t nf = R->S.nFluid, ncell = R->S.ncell;
+   const double* src = (R->S.pattern != 0 && R->cur) ? R->b : R->a;
+   const double nan = NAN;
+   for (int64_t k = 0; k < (int64_t)Q * ncell; k++) f_raw[k] = nan;
+   for (int64_t i = 0; i < nf; i++) {
+      int64_t c = R->S.fluidCell[i];
+      for (int s = 0; s < Q; s++) f_raw[(int64_t)s * ncell + c] = src[(int64_t)s * nf + i];
+   }
+   return 0;
+}
+
+/* create + step + read + destroy.  Returns 0 on success, 1 for bad
+ * arguments or allocation failure. */
 int lbm_oracle_run(int Q, int pattern, int compat_rest_weight, int nx, int ny, int nz,
                    const int* periodic, const unsigned char* solid, double omega,
                    const double* force, const double* force_field, const double* porosity,
                    const double* f_init, int nsteps, int nthreads, double* f_raw,
                    double* seconds)
 {
-   if (nx <= 0 || ny <= 0 || nz <= 0 || nsteps < 0 || pattern < 0 || pattern > 2) return 1;
-#ifdef _OPENMP
-   if (nthreads > 0) omp_set_num_threads(nthreads);
-#else
-   (void)nthreads;
-#endif
-   oracle_state S;
-   memset(&S, 0, sizeof(S));
-   int rc = build_state(&S, Q, pattern, compat_rest_weight, nx, ny, nz, periodic, solid);
-   if (rc) return rc;
-   S.omega = omega;
-   for (int d = 0; d < 3; d++) S.force[d] = force ? force[d] : 0.0;
-   S.forceField = force_field;
-   S.porosity = porosity;
-   const int64_t nf = S.nFluid;
-   const int64_t ncell = S.ncell;
-   double* a = (double*)malloc(sizeof(double) * (size_t)(nf > 0 ? nf : 1) * Q);
-   double* b = (double*)malloc(sizeof(double) * (size_t)(nf > 0 ? nf : 1) * Q);
-   if (!a || !b) {
-      free(a); free(b); free(S.fluidCell); free(S.adj);
-      return 2;
-   }
-   for (int64_t i = 0; i < nf; i++) {
-      int64_t c = S.fluidCell[i];
-      for (int s = 0; s < Q; s++) {
-         double v = f_init[(int64_t)s * ncell + c];
-         if (pattern == 0) {
-            a[(int64_t)S.L.opp[s] * nf + i] = v;
-         } else {
-            a[(int64_t)s * nf + i] = v;
-            b[(int64_t)s * nf + i] = v;
-         }
-      }
-   }
-   double* src = a;
-   double* tgt = b;
-   double t0 = now_seconds();
-   for (int t = 0; t < nsteps; t++) {
-      if (pattern == 0) {
-         if (t % 2 == 0) aa_even(&S, src);
-         else aa_odd(&S, src);
-      } else {
-         if (pattern == 1) ab_push(&S, src, tgt);
-         else ab_pull(&S, src, tgt);
-         double* tmp = src;
-         src = tgt;
-         tgt = tmp;
-      }
-   }
-   double t1 = now_seconds();
-   if (seconds) *seconds = t1 - t0;
-   const double nan = NAN;
-   for (int64_t k = 0; k < (int64_t)Q * ncell; k++) f_raw[k] = nan;
-   for (int64_t i = 0; i < nf; i++) {
-      int64_t c = S.fluidCell[i];
-      for (int s = 0; s < Q; s++) f_raw[(int64_t)s * ncell + c] = src[(int64_t)s * nf + i];
-   }
-   free(a);
-   free(b);
-   free(S.fluidCell);
-   free(S.adj);
-   return 0;
+   if (nsteps < 0) return 1;
+   void* R = lbm_oracle_create(Q, pattern, compat_rest_weight, nx, ny, nz, periodic, solid, omega,
+                               force, force_field, porosity, f_init, nthreads);
+   if (!R) return 1;
+   int rc = lbm_oracle_step(R, nsteps, seconds);
+   if (!rc) rc = lbm_oracle_read(R, f_raw);
+   lbm_oracle_destroy(R);
+   return rc;
 }

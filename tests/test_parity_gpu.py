@@ -87,7 +87,7 @@ def test_oracle_parity_walls_solids(gpu, Q, pattern, arithmetic, steps):
     assert rel_err(logical, ref_logical, m) <= max(tol, 1e-15)
     rr, ur = core.readout_macros(Q, pid, steps, ref, solid, per)
     fm = fluid_mask(solid)
-    assert rel_err(rho, rr, fm) < 1e-13
+    assert rel_err(rho, rr, fm) < (1e-13 if arithmetic == "f64" else 1e-11)
     assert rel_err(u, ur, np.broadcast_to(fm, u.shape)) < 1e-10
     c, _, _ = core.stencil(Q)
     mass = np.nansum(ref_logical[:, fm])
@@ -141,8 +141,9 @@ def test_shifted_storage_close_to_oracle(gpu, storage, tol, Q):
 
 
 def test_rest_state_is_invariant_and_mass_conserved(gpu):
-    """F = 0 rest state stays f = w bit for bit; the FP64 reduction gives the
-    fluid cell count as mass."""
+    """F = 0 rest state stays f = w (bit for bit with exact FP64 arithmetic,
+    to 1e-14 with F64X); the FP64 reduction gives the fluid cell count as
+    mass."""
     nx, ny, nz = 20, 12, 9
     solid = workloads.channel_mask(nx, ny, nz)
     for arith in ("f64", "f64x"):
@@ -154,7 +155,10 @@ def test_rest_state_is_invariant_and_mass_conserved(gpu):
             sim.step(6)
             f = sim.get_populations("logical")
             m = fluid_mask(solid, 19)
-            assert np.array_equal(f[m], f_init[m])
+            if arith == "f64":
+                assert np.array_equal(f[m], f_init[m])
+            else:
+                assert rel_err(f, f_init, m) < 1e-14
             cons = sim.conserved()
             assert cons[0] == pytest.approx(sim.nfluid, rel=1e-14)
             assert np.all(np.abs(cons[1:]) < 1e-12)
