@@ -20,6 +20,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "liblbm_gb300.so"
+APP = PKG / "lbm-gb300-app"
 
 SOURCES = [
     "lbm_api.cu",
@@ -47,6 +48,7 @@ def nvcc() -> str:
 def _inputs():
     files = [CSRC / s for s in SOURCES]
     files += sorted(CSRC.glob("*.cuh"))
+    files.append(PKG / "app" / "lbm_app.cpp")
     files.append(ROOT / "include" / "lbm_gb300.h")
     return files
 
@@ -82,7 +84,22 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_app()
     return LIB
+
+
+def build_app() -> Path:
+    """The C++ drop-in driver (app/lbm_app.cpp), linked against the library
+    with an $ORIGIN rpath so it runs from the package directory."""
+    src = PKG / "app" / "lbm_app.cpp"
+    tmp = APP.with_name(APP.name + f".tmp{os.getpid()}")
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(src),
+           "-L", str(PKG), "-llbm_gb300", "-Wl,-rpath,$ORIGIN", "-o", str(tmp)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"app build failed:\n{r.stderr}")
+    os.replace(tmp, APP)
+    return APP
 
 
 if __name__ == "__main__":

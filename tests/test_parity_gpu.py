@@ -143,7 +143,8 @@ def test_shifted_storage_close_to_oracle(gpu, storage, tol, Q):
 def test_rest_state_is_invariant_and_mass_conserved(gpu):
     """F = 0 rest state stays f = w: with exact FP64 arithmetic bit for bit
     equal to the oracle (the reference itself drifts in the last bit because
-    sum(w) rounds away from 1.0), with F64X within 1e-14; the FP64 reduction
+    sum(w) rounds away from 1.0), with F64X within 1e-13 (about 2^-46 per
+    step); the FP64 reduction
     gives the fluid cell count as mass."""
     nx, ny, nz = 20, 12, 9
     solid = workloads.channel_mask(nx, ny, nz)
@@ -159,7 +160,7 @@ def test_rest_state_is_invariant_and_mass_conserved(gpu):
             if arith == "f64":
                 ref, _ = core.run(19, core.AA, f_init, 6, 1.3, (0, 0, 0), (1, 0, 1), solid)
                 assert np.array_equal(f[m], core.raw_to_logical(19, core.AA, 6, ref, solid, (1, 0, 1))[m])
-            assert rel_err(f, f_init, m) < 1e-14
+            assert rel_err(f, f_init, m) < 1e-13
             cons = sim.conserved()
             assert cons[0] == pytest.approx(sim.nfluid, rel=1e-14)
             assert np.all(np.abs(cons[1:]) < 1e-12)
