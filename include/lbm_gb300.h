@@ -173,6 +173,29 @@ lbm_status lbm_timestep_force(lbm_handle* h, const void* src, void* tgt, int64_t
  * lbm_get_populations reads). */
 lbm_status lbm_population_buffer(lbm_handle* h, void** dev_ptr);
 
+/* ---- allocation-free conservation reduction.  No counterpart in the
+ * reference.  For callers that cannot allocate device memory while they run
+ * (hosts that give every device byte to their own pool at start-up, drivers
+ * that must not allocate inside their time loop) and therefore cannot create a
+ * handle.  Everything is caller-owned device memory: dstrb (a population
+ * buffer in the raw layout of the given storage, plane_stride elements per
+ * direction), solid (ncell bytes, nonzero = solid; NULL = none) and out (4
+ * doubles: mass, momentum x/y/z, as lbm_reduce_conserved).  periodic is a
+ * host array of 3 flags.  readout: 0 = slot s holds direction s (AB push),
+ * 1 = AA at even time (slot opp(s)), 2 = pull gather (AA at odd time, AB
+ * pull).  Asynchronous on `stream` (cudaStream_t as void*, NULL = legacy
+ * default stream), on the current device; out is not checked for NaN/Inf.
+ * Calls no cudaMalloc: the per-block partial sums live in a static device
+ * array of 512 KiB that every GPU loading the library keeps until exit, so at
+ * most 2^28 (268,435,456) cells are accepted; larger grids return
+ * LBM_ERR_INVALID_ARGUMENT.  The first call on each device looks the array's
+ * address up (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the array: calls that
+ * overlap on the GPU race. */
+lbm_status lbm_reduce_conserved_noalloc(int lattice, int storage, int nx, int ny, int nz,
+                                        int64_t plane_stride, const void* dstrb, const uint8_t* solid,
+                                        const int periodic[3], int readout, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

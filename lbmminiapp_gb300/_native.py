@@ -74,6 +74,7 @@ _SIGNATURES = {
     "lbm_timestep_odd_force": (ctypes.c_int, [_P, _P, _I64, _I64]),
     "lbm_timestep_force": (ctypes.c_int, [_P, _P, _P, _I64, _I64]),
     "lbm_population_buffer": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "lbm_reduce_conserved_noalloc": (ctypes.c_int, [ctypes.c_int] * 5 + [_I64, _P, _P, _P, ctypes.c_int, _P, _P]),
 }
 
 _lib = None

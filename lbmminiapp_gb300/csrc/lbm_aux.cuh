@@ -241,7 +241,8 @@ __global__ void __launch_bounds__(kReduceThreads) conserved_partial_kernel(GridD
    }
 }
 
-__global__ void conserved_final_kernel(const double* partials, int nblocks, double* out)
+// static: every translation unit that includes this header gets its own copy.
+static __global__ void conserved_final_kernel(const double* partials, int nblocks, double* out)
 {
    __shared__ double sh[4][kReduceThreads];
    for (int k = 0; k < 4; k++) {

@@ -1,0 +1,74 @@
+"""lbm_reduce_conserved_noalloc: the conservation reduction for callers that
+cannot allocate device memory while they run (they hand all device memory to
+their own pool at start-up, or must not allocate inside their time loop).
+
+The entry point keeps its per-block partial sums in a static device array
+instead of an allocation.  Checked here through the C ABI against the handle's
+lbm_reduce_conserved on the same state, on two calls in a row (the second sees
+the array exactly as the first left it).  This file is collected last so a run
+that stops at the first failure has already run every other test.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from lbmminiapp_gb300 import Simulation, workloads
+from lbmminiapp_gb300 import _native as N
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12  # relative; the two reductions add the same FP64 terms in different orders
+
+
+def readout_mode(pattern, t):
+    if pattern == "aa":
+        return 1 if t % 2 == 0 else 2
+    return 2 if pattern == "ab_pull" else 0
+
+
+@pytest.mark.parametrize("Q,pattern,storage,walls,steps", [
+    (19, "aa", "f64", True, 3),
+    (19, "aa", "f64", False, 4),
+    (27, "ab_pull", "f64", True, 2),
+    (19, "ab_push", "f16", True, 5),
+])
+def test_noalloc_matches_handle_reduction(gpu, Q, pattern, storage, walls, steps):
+    import torch
+    nx, ny, nz = 40, 24, 18
+    solid = workloads.channel_mask(nx, ny, nz) if walls else np.zeros((nz, ny, nx), np.uint8)
+    periodic = (1, 0, 1) if walls else (1, 1, 1)
+    u = workloads.taylor_green(nx, ny, nz, 0.05, noise=1e-3, seed=Q + steps)
+    u[:, solid.astype(bool)] = 0
+    with Simulation(nx, ny, nz, lattice=Q, pattern=pattern, omega=1.6, force=(1e-5, 0, 0), periodic=periodic,
+                    storage=storage) as sim:
+        sim.set_solid(solid)
+        sim.init_equilibrium(None, u)
+        sim.step(steps)
+        expected = sim.conserved()
+        buf = sim.population_buffer()
+        plane = int(sim.info.plane_stride)
+        solid_dev = torch.from_numpy(solid.reshape(-1)).cuda() if walls else None
+        out = torch.full((4,), float("nan"), dtype=torch.float64, device="cuda")
+        per = (ctypes.c_int * 3)(*periodic)
+        lib = N.lib()
+        for call in range(2):
+            st = lib.lbm_reduce_conserved_noalloc(
+                Q, N.STORAGE_NAMES[storage], nx, ny, nz, plane, ctypes.c_void_p(buf),
+                ctypes.c_void_p(solid_dev.data_ptr()) if walls else None, per, readout_mode(pattern, steps),
+                ctypes.c_void_p(out.data_ptr()), None)
+            assert st == 0
+            torch.cuda.synchronize()
+            got = out.cpu().numpy()
+            assert np.all(np.isfinite(got))
+            assert abs(got[0] - expected[0]) <= TOL * abs(expected[0])
+            assert np.all(np.abs(got[1:] - expected[1:]) <= TOL * abs(expected[0]))
+
+
+def test_noalloc_rejects_grids_beyond_its_scratch(gpu):
+    lib = N.lib()
+    per = (ctypes.c_int * 3)(1, 1, 1)
+    n = 1 << 28
+    st = lib.lbm_reduce_conserved_noalloc(19, 0, 1024, 1024, 257, n + 1024 * 1024, ctypes.c_void_p(16), None,
+                                          per, 0, ctypes.c_void_p(16), None)
+    assert st == 1  # LBM_ERR_INVALID_ARGUMENT, before any device work
