@@ -156,6 +156,20 @@ KParams make_params(const lbm_handle* h, int64_t start, int64_t end, Launch& L)
       split(c.omega * w, p.x_ow[k]);
    }
    for (int d = 0; d < 3; d++) split(c.force[d], p.x_F[d]);
+   for (int s = 0; s < h->Q; s++) {
+      const double cf = 3.0 * (lat_c(h->Q, s, 0) * c.force[0] + lat_c(h->Q, s, 1) * c.force[1] +
+                               lat_c(h->Q, s, 2) * c.force[2]);
+      split(p.om2 * lat_w(h->Q, s) * cf, p.x_Kf[s]);
+   }
+   for (int d = 0; d < 3; d++) split(3.0 * c.force[d], p.x_F3[d]);
+   for (int k = 0; k < 4; k++) {
+      double w;
+      if (h->Q == 19) w = k == 0 ? 1.0 / 3.0 : (k == 1 ? 1.0 / 18.0 : 1.0 / 36.0);
+      else w = k == 0 ? 8.0 / 27.0 : (k == 1 ? 2.0 / 27.0 : (k == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+      split(p.om2 * w, p.x_om2w[k]);
+   }
+   split(p.om2 / 36.0, p.x_om2w36);
+   p.forced = (c.force[0] != 0.0 || c.force[1] != 0.0 || c.force[2] != 0.0) ? 1 : 0;
    int bx = (int)std::min<int64_t>(256, ((c.nx + 31) / 32) * 32);
    L.block = dim3(bx, 1, 1);
    L.grid = dim3((c.nx + bx - 1) / bx, c.ny, (unsigned)(z1 - z0));

@@ -283,140 +283,238 @@ struct Consts {
    df omega;
    df ow[4];      // omega * w for |c|^2 = 0, 1, 2, 3
    df F[3];       // uniform body force
-   float om2;     // 1 - omega/2 (multiplies only the small forcing terms)
+   df F3[3];      // 3 F
+   df Kf[27];     // (1 - omega/2) w_s 3 c_s.F per direction: the forcing term linear in F
+   df om2w[4];    // (1 - omega/2) w per weight class
+   df om2w36;     // (1 - omega/2) / 36 (rest weight of the Q19 AA Unroll kernels)
+   float om2;
 };
 
 }  // namespace x64
 
+// Representative s < opp(s) of the p-th opposite pair (direction order of
+// the reference: pairs are (0,1), (2,3), ... with the rest direction last).
+__host__ __device__ constexpr int pair_dir(int Q, int p)
+{
+   int seen = 0;
+   for (int s = 0; s < Q; s++) {
+      if (s < lat_opp(Q, s)) {
+         if (seen == p) return s;
+         seen++;
+      }
+   }
+   return -1;
+}
+
+// Fast-path validity thresholds (high words of the doubles).
+constexpr uint32_t kHiQuarter = (uint32_t)(1023 - 2) << 20;   // 0.25
+
 // The fast-path collision on one cell.  bits[] holds the Q input patterns in
 // direction order and receives the Q output patterns.  Returns false (leaving
-// bits[] untouched) when the cell must take the exact path.
-template <int Q>
+// bits[] untouched) when the cell must take the exact path:
+//   * inputs: rest population in [0.25, 1), the others in [2^-80, 0.25) --
+//     so rho's running sum, started at the rest population, always has an
+//     exponent at least that of the next term (Fast2Sum is exact);
+//   * |3 v_d| < 0.3: |c.u| stays well below 1 - uu/2, so the pair sums
+//     (1 - uu/2 + cu^2/2) +- cu keep their larger operand first;
+//   * outputs inside [2^-80, 1).
+// Work is organised by opposite pairs (s, opp(s)): cu, the quadratic term and
+// the omega*w*rho products are shared, since cu(opp) = -cu(s).
+template <int Q, bool FORCE>
 __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], const x64::Consts& k,
                                                           int compat)
 {
    using namespace x64;
+   constexpr int R = lat_rest(Q);
+   constexpr int NP = (Q - 1) / 2;
    uint32_t hmin = 0xFFFFFFFFu, hmax = 0;
 #pragma unroll
    for (int s = 0; s < Q; s++) {
+      if (s == R) continue;
       const uint32_t hi = (uint32_t)(bits[s] >> 32);
       hmin = hmin < hi ? hmin : hi;
       hmax = hmax > hi ? hmax : hi;
    }
-   if (hmin < kHiMin || hmax >= kHiMax) return false;
+   const uint32_t hr = (uint32_t)(bits[R] >> 32);
+   if (hmin < kHiMin || hmax >= kHiQuarter || hr < kHiQuarter || hr >= kHiMax) return false;
 
    df f[Q];
 #pragma unroll
    for (int s = 0; s < Q; s++) f[s] = split(bits[s]);
 
-   // rho: start from the rest population (the largest) so every partial sum
-   // dominates the next term and Fast2Sum is exact.
-   constexpr int R = lat_rest(Q);
-   df rho = f[R];
+   // rho = f_rest + sum of the rest (Fast2Sum chain, exact by the range check);
+   // the low word is folded back every 6 terms so it stays near ulp(rho).
+   float rh = f[R].h, rl = f[R].l;
 #pragma unroll
    for (int s = 0; s < Q; s++) {
       if (s == R) continue;
-      const df t = fast_two_sum(rho.h, f[s].h);
-      rho = {t.h, fadd(rho.l, fadd(t.l, f[s].l))};
+      const float t = fadd(rh, f[s].h);
+      rl = fadd(rl, fadd(fsub(f[s].h, fsub(t, rh)), f[s].l));
+      rh = t;
+      if (s % 6 == 5) {
+         const df n = fast_two_sum(rh, rl);
+         rh = n.h;
+         rl = n.l;
+      }
    }
-   rho = fast_two_sum(rho.h, rho.l);
+   const df rho = fast_two_sum(rh, rl);
 
-   // j = sum c f per component (TwoSum: partial sums may cancel).
-   df j[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+   // j = sum over pairs of c_s (f_s - f_opp(s)), differences by TwoSum
+   df D[NP];
+#pragma unroll
+   for (int q = 0; q < NP; q++) {
+      const int s = pair_dir(Q, q), o = lat_opp(Q, s);
+      const df t = two_sum(f[s].h, -f[o].h);
+      D[q] = {t.h, fadd(t.l, fsub(f[s].l, f[o].l))};
+   }
+   df j[3];
 #pragma unroll
    for (int d = 0; d < 3; d++) {
+      float jh = 0.f, jl = 0.f;
       bool first = true;
 #pragma unroll
-      for (int s = 0; s < Q; s++) {
-         const int c = lat_c(Q, s, d);
+      for (int q = 0; q < NP; q++) {
+         const int c = lat_c(Q, pair_dir(Q, q), d);
          if (c == 0) continue;
-         const df term = c > 0 ? f[s] : df_neg(f[s]);
+         const float th = c > 0 ? D[q].h : -D[q].h;
+         const float tl = c > 0 ? D[q].l : -D[q].l;
          if (first) {
-            j[d] = term;
+            jh = th;
+            jl = tl;
             first = false;
          } else {
-            const df t = two_sum(j[d].h, term.h);
-            j[d] = {t.h, fadd(j[d].l, fadd(t.l, term.l))};
+            const df t = two_sum(jh, th);
+            jh = t.h;
+            jl = fadd(jl, fadd(t.l, tl));
+            if (q % 4 == 3) {
+               const df n = fast_two_sum(jh, jl);
+               jh = n.h;
+               jl = n.l;
+            }
          }
       }
-      j[d] = fast_two_sum(j[d].h, j[d].l);
+      j[d] = fast_two_sum(jh, jl);
    }
 
-   // v = (j + F/2) / rho; the force is small, so F/2 enters the low word
-   // after an exact Fast2Sum of the high words.
-   const df* F = k.F;
+   // v = (j + F/2) / rho
    const float r0 = frcp(rho.h);
    float e = ffma(-rho.h, r0, 1.0f);
    e = ffma(-rho.l, r0, e);
    const df inv = {r0, fmul(r0, e)};
-   df v[3];
+   df v[3], v3[3];
 #pragma unroll
    for (int d = 0; d < 3; d++) {
-      const df jf = df_add(j[d], {0.5f * F[d].h, 0.5f * F[d].l});
+      const df jf = df_add(j[d], {0.5f * k.F[d].h, 0.5f * k.F[d].l});
       v[d] = df_mul(jf, inv);
-   }
-   // 3 v (the factor 3 of cu and uu folded in once).
-   df v3[3];
-#pragma unroll
-   for (int d = 0; d < 3; d++) {
       const float p = fmul(3.0f, v[d].h);
       v3[d] = fast_two_sum(p, ffma(3.0f, v[d].h, -p) + 3.0f * v[d].l);
    }
-   // uu = 3 v.v ;  base = 1 - uu/2
+   if (!(fabsf(v3[0].h) < 0.3f && fabsf(v3[1].h) < 0.3f && fabsf(v3[2].h) < 0.3f)) return false;
+   // uu = 3 v.v
    df uu = df_mul_u(v3[0], v[0]);
    uu = df_add(uu, df_mul_u(v3[1], v[1]));
    uu = df_add(uu, df_mul_u(v3[2], v[2]));
    const df base = df_add_fast({1.0f, 0.0f}, {-0.5f * uu.h, -0.5f * uu.l});
-   const float fu = 3.0f * (F[0].h * v[0].h + F[1].h * v[1].h + F[2].h * v[2].h);
+   // fu = 3 F.v (float pair; zero without a force)
+   df fu = {0.f, 0.f};
+   if (FORCE) {
+      fu = df_mul_u(k.F3[0], v[0]);
+      fu = df_add(fu, df_mul_u(k.F3[1], v[1]));
+      fu = df_add(fu, df_mul_u(k.F3[2], v[2]));
+   }
 
-   // omega * w * rho per weight class, folded into one factor.
    df owr[4];
 #pragma unroll
    for (int cls = 0; cls < 4; cls++) owr[cls] = df_mul(k.ow[cls], rho);
 
-   df out[Q];
+   // Results are written back only after every output passed its check (a
+   // fallback must still see the original inputs).
+   uint64_t res[Q - 1];
+   uint64_t rest_bits;
+   // rest direction: P = base
+   {
+      const df A = df_mul_u(owr[0], base);
+      const df a = df_mul_u(k.om1, f[R]);
+      const df t = two_sum(A.h, a.h);
+      df out = {t.h, fadd(t.l, fadd(A.l, a.l))};
+      if (FORCE) {
+         // -(1 - omega/2) wf fu, wf = 1/36 with the Unroll-kernel weights
+         const df fr = df_mul_u(compat ? k.om2w36 : k.om2w[0], fu);
+         const df t2 = two_sum(out.h, -fr.h);
+         out = {t2.h, fadd(t2.l, fsub(out.l, fr.l))};
+      }
+      if (!out_ok(out)) return false;
+      rest_bits = join(out);
+   }
 #pragma unroll
-   for (int s = 0; s < Q; s++) {
+   for (int q = 0; q < NP; q++) {
+      const int s = pair_dir(Q, q), o = lat_opp(Q, s);
       const int c0 = lat_c(Q, s, 0), c1 = lat_c(Q, s, 1), c2 = lat_c(Q, s, 2);
       const int cls = lat_norm2(Q, s);
-      // cu = 3 c.v as a double-float
+      // cu = 3 c_s.v (two_sum-based, left unnormalised)
       df cu = {0.f, 0.f};
       bool first = true;
       if (c0 != 0) { cu = c0 > 0 ? v3[0] : df_neg(v3[0]); first = false; }
       if (c1 != 0) {
          const df t = c1 > 0 ? v3[1] : df_neg(v3[1]);
-         cu = first ? t : df_add(cu, t);
-         first = false;
+         if (first) { cu = t; first = false; }
+         else { const df u2 = two_sum(cu.h, t.h); cu = {u2.h, fadd(u2.l, fadd(cu.l, t.l))}; }
       }
       if (c2 != 0) {
          const df t = c2 > 0 ? v3[2] : df_neg(v3[2]);
-         cu = first ? t : df_add(cu, t);
-         first = false;
+         if (first) { cu = t; first = false; }
+         else { const df u2 = two_sum(cu.h, t.h); cu = {u2.h, fadd(u2.l, fadd(cu.l, t.l))}; }
       }
-      // P = 1 + cu + cu^2/2 - uu/2 = (base + cu^2/2) + cu
-      df P = base;
-      if (!first) {
-         const df c2h = df_sqr_u(cu);
-         P = df_add_fast(P, {0.5f * c2h.h, 0.5f * c2h.l});
-         P = df_add_fast(P, cu);
+      // Qp = base + cu^2 / 2
+      const df c2h = df_sqr_u(cu);
+      const df qs = fast_two_sum(base.h, 0.5f * c2h.h);
+      const df Qp = {qs.h, fadd(qs.l, fadd(base.l, 0.5f * c2h.l))};
+      const df A = df_mul_u(owr[cls], Qp);   // omega * eq, symmetric part
+      const df B = df_mul_u(owr[cls], cu);   // omega * eq, antisymmetric part
+      // forcing om2 w (+-cf - fu + cu cf) = +-Kf[s] + (Kf[s] cu - om2 w fu), with
+      // Kf[s] = om2 w cf a float pair made on the host
+      df sym = {0.f, 0.f};
+      if (FORCE) {
+         const df gc = df_mul_u(k.Kf[s], cu);
+         const df wf = df_mul_u(k.om2w[cls], fu);
+         const df t3 = two_sum(gc.h, -wf.h);
+         sym = {t3.h, fadd(t3.l, fsub(gc.l, wf.l))};
       }
-      const df eqw = df_mul_u(owr[cls], P);  // omega * eq_s
-      // forcing: (1 - omega/2) wf (cf - fu + cu cf), small: single precision
-      const float cf = 3.0f * ((float)c0 * F[0].h + (float)c1 * F[1].h + (float)c2 * F[2].h);
-      float wf = (float)lat_w(Q, s);
-      if (Q == 19 && s == R && compat) wf = (float)(1.0 / 36.0);
-      const float frc = k.om2 * wf * (cf - fu + cu.h * cf);
-      // (1 - omega) f_s + omega eq_s + forcing
-      const df a = df_mul_u(k.om1, f[s]);
-      const df t = two_sum(a.h, eqw.h);
-      out[s] = {t.h, fadd(t.l, fadd(fadd(a.l, eqw.l), frc))};
+      // s: A + B ; opp(s): A - B ; then + (1 - omega) f
+      {
+         const df tp = fast_two_sum(A.h, B.h);
+         const df a = df_mul_u(k.om1, f[s]);
+         const df t = two_sum(tp.h, a.h);
+         df out = {t.h, fadd(t.l, fadd(tp.l, fadd(fadd(A.l, B.l), a.l)))};
+         if (FORCE) {
+            const df fr = two_sum(k.Kf[s].h, sym.h);
+            const df t2 = two_sum(out.h, fr.h);
+            out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fadd(k.Kf[s].l, sym.l))))};
+         }
+         if (!out_ok(out)) return false;
+         res[q] = join(out);
+      }
+      {
+         const df tm = fast_two_sum(A.h, -B.h);
+         const df a = df_mul_u(k.om1, f[o]);
+         const df t = two_sum(tm.h, a.h);
+         df out = {t.h, fadd(t.l, fadd(tm.l, fadd(fsub(A.l, B.l), a.l)))};
+         if (FORCE) {
+            const df fr = two_sum(sym.h, -k.Kf[s].h);
+            const df t2 = two_sum(out.h, fr.h);
+            out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fsub(sym.l, k.Kf[s].l))))};
+         }
+         if (!out_ok(out)) return false;
+         res[NP + q] = join(out);
+      }
    }
-   bool ok = true;
 #pragma unroll
-   for (int s = 0; s < Q; s++) ok = ok && out_ok(out[s]);
-   if (!ok) return false;
-#pragma unroll
-   for (int s = 0; s < Q; s++) bits[s] = join(out[s]);
+   for (int q = 0; q < NP; q++) {
+      const int s = pair_dir(Q, q);
+      bits[s] = res[q];
+      bits[lat_opp(Q, s)] = res[NP + q];
+   }
+   bits[R] = rest_bits;
    return true;
 }
 
@@ -432,8 +530,17 @@ __device__ __forceinline__ void collide_f64x(uint64_t (&bits)[Q], const KParams&
    for (int c = 0; c < 4; c++) k.ow[c] = {p.x_ow[c][0], p.x_ow[c][1]};
 #pragma unroll
    for (int d = 0; d < 3; d++) k.F[d] = {p.x_F[d][0], p.x_F[d][1]};
+#pragma unroll
+   for (int d = 0; d < 3; d++) k.F3[d] = {p.x_F3[d][0], p.x_F3[d][1]};
+#pragma unroll
+   for (int s = 0; s < Q; s++) k.Kf[s] = {p.x_Kf[s][0], p.x_Kf[s][1]};
+#pragma unroll
+   for (int c = 0; c < 4; c++) k.om2w[c] = {p.x_om2w[c][0], p.x_om2w[c][1]};
+   k.om2w36 = {p.x_om2w36[0], p.x_om2w36[1]};
    k.om2 = p.om2f;
-   if (collide_f64x_fast<Q>(bits, k, p.compat)) return;
+   const bool fast = p.forced ? collide_f64x_fast<Q, true>(bits, k, p.compat)
+                              : collide_f64x_fast<Q, false>(bits, k, p.compat);
+   if (fast) return;
    double d[Q], o[Q];
 #pragma unroll
    for (int s = 0; s < Q; s++) d[s] = x64::as_double(bits[s]);

@@ -51,6 +51,11 @@ struct KParams {
    float x_om1[2], x_omega[2];
    float x_ow[4][2];              // omega * w per weight class (|c|^2 = 0..3)
    float x_F[3][2];               // uniform force
+   float x_Kf[27][2];             // (1 - omega/2) w_s 3 c_s.F per direction
+   float x_F3[3][2];              // 3 F
+   float x_om2w[4][2];            // (1 - omega/2) w per weight class
+   float x_om2w36[2];             // (1 - omega/2) / 36
+   int forced;                    // uniform force nonzero
 };
 
 // Link word: bit s set when the neighbour at x + c_s is solid or outside a

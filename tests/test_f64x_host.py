@@ -1,0 +1,105 @@
+"""F64X collision compiled for the host: precision against the exact IEEE
+double collision and the conditions that send a cell to the exact path.
+CPU only (nvcc builds host code without a GPU)."""
+import ctypes
+import shutil
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import core
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def f64x(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(nvcc).exists():
+        pytest.skip("nvcc not available")
+    out = tmp_path_factory.mktemp("f64x") / "libf64x_host.so"
+    subprocess.run([nvcc, "-O2", "-std=c++17", "--expt-relaxed-constexpr", "-shared", "-Xcompiler", "-fPIC",
+                    "-I", str(ROOT / "lbmminiapp_gb300" / "csrc"), str(ROOT / "tests" / "native" / "f64x_host_check.cu"),
+                    "-o", str(out)], check=True)
+    lib = ctypes.CDLL(str(out))
+    P = ctypes.c_void_p
+    lib.f64x_collide_host.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_double, P, ctypes.c_int, P]
+    return lib
+
+
+def collide_exact(Q, f, omega, F, compat=False):
+    """Reference BGK + Guo collision (src/kernels/KernelAA_SOA_Base.cpp:186-247), cells along axis 0."""
+    c, _, w = core.stencil(Q)
+    wf = w.copy()
+    if compat and Q == 19:
+        wf[18] = 1.0 / 36.0
+    rho = f.sum(axis=1)
+    v = (f @ c.astype(float) + 0.5 * np.asarray(F)) / rho[:, None]
+    vv = 3.0 * (v * v).sum(axis=1)
+    fv = 3.0 * (v @ np.asarray(F))
+    cu = 3.0 * v @ c.T.astype(float)
+    cf = 3.0 * (c.astype(float) @ np.asarray(F))
+    eq = w * rho[:, None] * (1.0 + cu + 0.5 * cu * cu - 0.5 * vv[:, None])
+    fd = wf * (cf - fv[:, None] + cu * cf)
+    return (1.0 - omega) * f + omega * eq + (1.0 - 0.5 * omega) * fd
+
+
+def random_cells(Q, n, U, neq, seed):
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(-U, U, (3, n))
+    rho = 1.0 + rng.uniform(-0.01, 0.01, n)
+    f = core.equilibrium(Q, rho, u).T.copy()
+    f *= 1.0 + neq * rng.standard_normal(f.shape)
+    return f
+
+
+def run(lib, Q, f, omega, F, compat=0):
+    f = np.ascontiguousarray(f)
+    out = np.empty_like(f)
+    fast = np.empty(f.shape[0], np.int32)
+    Fa = np.asarray(F, dtype=np.float64)
+    lib.f64x_collide_host(Q, f.ctypes.data, out.ctypes.data, f.shape[0], omega, Fa.ctypes.data, compat,
+                          fast.ctypes.data)
+    return out, fast.astype(bool)
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+@pytest.mark.parametrize("omega", [1.0 / 0.55, 1.25, 1.0, 0.7])
+@pytest.mark.parametrize("F", [(0.0, 0.0, 0.0), (1e-5, -2e-6, 3e-6)])
+def test_fast_path_matches_exact_collision(f64x, Q, omega, F):
+    f = random_cells(Q, 4000, 0.08, 0.02, seed=Q)
+    out, fast = run(f64x, Q, f, omega, F)
+    assert fast.mean() > 0.99
+    ref = collide_exact(Q, f, omega, F)
+    err = np.abs(out[fast] - ref[fast]) / np.abs(ref[fast])
+    assert err.max() < 2e-13, err.max()        # per step, per population (relative)
+    assert np.median(err) < 2e-14
+
+
+def test_compat_rest_weight(f64x):
+    f = random_cells(19, 500, 0.05, 0.01, seed=3)
+    F = (1e-5, 0.0, 0.0)
+    out, fast = run(f64x, 19, f, 1.3, F, compat=1)
+    ref = collide_exact(19, f, 1.3, F, compat=True)
+    assert fast.all()
+    assert (np.abs(out - ref) / np.abs(ref)).max() < 2e-13
+
+
+@pytest.mark.parametrize("case", ["zero", "negative", "above_one", "fast_flow", "nan"])
+def test_out_of_range_cells_take_the_exact_path(f64x, case):
+    f = random_cells(19, 8, 0.02, 0.0, seed=5)
+    if case == "zero":
+        f[3, 7] = 0.0
+    elif case == "negative":
+        f[3, 7] = -1e-3
+    elif case == "above_one":
+        f[3, 18] = 1.5
+    elif case == "nan":
+        f[3, 2] = np.nan
+    else:
+        f[3] = core.equilibrium(19, np.ones(1), np.array([[0.15], [0.0], [0.0]]))[:, 0]
+    _, fast = run(f64x, 19, f, 1.2, (0, 0, 0))
+    assert not fast[3]
+    assert fast[[0, 1, 2, 4, 5, 6, 7]].all()
