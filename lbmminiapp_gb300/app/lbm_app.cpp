@@ -149,7 +149,8 @@ int main(int argc, char** argv)
       const double vel = u[c];
       std::cout << ((vel - expected) / expected < 0.25 ? "Passed baseline validation" : "Failed baseline validation")
                 << std::endl;
-      std::cout << "Centre-line velocity " << vel << " (Poiseuille " << expected << ")" << std::endl;
+      std::printf("Centre-line velocity %.17g (Poiseuille %.17g)\n", vel, expected);
+      std::fflush(stdout);
    }
    lbm_destroy(h);
    const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - tStart).count();

@@ -63,6 +63,8 @@ def up_to_date() -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     if not force and up_to_date():
+        if not APP.exists():
+            build_app()
         return LIB
     BUILD.mkdir(exist_ok=True)
     cc = nvcc()

@@ -12,6 +12,7 @@ namespace lbm {
 struct Launch {
    dim3 grid, block;
    cudaStream_t stream;
+   bool idx32;   // Q * plane < 2^32: 32-bit slot indices
 };
 
 template <int Q, int ST, int AR, int KIND>
@@ -23,12 +24,18 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
    T* d = static_cast<T*>(dst);
    // Per-cell fields always use the exact FP64 arithmetic when FP64 is stored.
    constexpr int ARF = (AR == AR_F64X) ? AR_F64 : AR;
-   if (links) {
-      if (fields) step_kernel<Q, ST, ARF, KIND, true, true><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
-      else step_kernel<Q, ST, AR, KIND, true, false><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+   // Per-cell fields (porosity, force field) are the adjoint / research
+   // configurations: 64-bit indices only.  The plain step kernels get a 32-bit
+   // index variant for buffers of fewer than 2^32 elements.
+   if (fields) {
+      if (links) step_kernel<Q, ST, ARF, KIND, true, true, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+      else step_kernel<Q, ST, ARF, KIND, false, true, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+   } else if (L.idx32) {
+      if (links) step_kernel<Q, ST, AR, KIND, true, false, uint32_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+      else step_kernel<Q, ST, AR, KIND, false, false, uint32_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
    } else {
-      if (fields) step_kernel<Q, ST, ARF, KIND, false, true><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
-      else step_kernel<Q, ST, AR, KIND, false, false><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+      if (links) step_kernel<Q, ST, AR, KIND, true, false, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+      else step_kernel<Q, ST, AR, KIND, false, false, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
    }
    return cudaGetLastError();
 }

@@ -242,6 +242,21 @@ __host__ __device__ __forceinline__ uint64_t join(df v)
    return d0 + (uint64_t)((int64_t)ei * 128);
 }
 
+// join() plus the output range check on S, the float rounding of the result:
+// ok becomes false unless 2^-80 <= S < 1 (positive, inside the fast range).
+__host__ __device__ __forceinline__ uint64_t join_checked(df v, bool& ok)
+{
+   const float S = fadd_rz(v.h, v.l);
+   const float E = fsub(v.l, fsub(S, v.h));
+   const uint32_t sb = fbits(S);
+   ok = ok && (sb - 0x17800000u) < (0x3F800000u - 0x17800000u);
+   const float scale = bitsf(0x95800000u - (sb & 0x7F800000u));  // 2^(45 - e(S))
+   const float y = ffma(E, scale, 12582912.0f);
+   const int32_t ei = (int32_t)(fbits(y) - 0x4B400000u);
+   const uint64_t d0 = ((uint64_t)sb << 29) + ((uint64_t)0x38000000u << 32);
+   return d0 + (uint64_t)((int64_t)ei * 128);
+}
+
 __host__ __device__ __forceinline__ bool in_range(uint64_t bits)
 {
    const uint32_t hi = (uint32_t)(bits >> 32);
@@ -431,6 +446,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
    // fallback must still see the original inputs).
    uint64_t res[Q - 1];
    uint64_t rest_bits;
+   bool ok = true;
    // rest direction: P = base
    {
       const df A = df_mul_u(owr[0], base);
@@ -443,8 +459,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
          const df t2 = two_sum(out.h, -fr.h);
          out = {t2.h, fadd(t2.l, fsub(out.l, fr.l))};
       }
-      if (!out_ok(out)) return false;
-      rest_bits = join(out);
+      rest_bits = join_checked(out, ok);
    }
 #pragma unroll
    for (int q = 0; q < NP; q++) {
@@ -491,8 +506,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
             const df t2 = two_sum(out.h, fr.h);
             out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fadd(k.Kf[s].l, sym.l))))};
          }
-         if (!out_ok(out)) return false;
-         res[q] = join(out);
+         res[q] = join_checked(out, ok);
       }
       {
          const df tm = fast_two_sum(A.h, -B.h);
@@ -504,10 +518,10 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
             const df t2 = two_sum(out.h, fr.h);
             out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fsub(sym.l, k.Kf[s].l))))};
          }
-         if (!out_ok(out)) return false;
-         res[NP + q] = join(out);
+         res[NP + q] = join_checked(out, ok);
       }
    }
+   if (!ok) return false;
 #pragma unroll
    for (int q = 0; q < NP; q++) {
       const int s = pair_dir(Q, q);

@@ -24,10 +24,12 @@
 
 namespace lbm {
 
+// Cell and slot indices: IT is uint32_t when Q * plane < 2^32 (one IMAD per
+// slot index, one IMAD.WIDE per address), int64_t otherwise.  Cell indices and
+// neighbour offsets always fit 32 bits (fewer than 2^31 cells per handle).
 struct CellIndex {
    int64_t c;
-   int dxm, dxp, dym, dyp;   // neighbour offsets in cells along x and y
-   int64_t dzm, dzp;
+   int dxm, dxp, dym, dyp, dzm, dzp;   // neighbour offsets in cells
 };
 
 __device__ __forceinline__ bool cell_of_thread(const KParams& p, CellIndex& ci)
@@ -43,50 +45,53 @@ __device__ __forceinline__ bool cell_of_thread(const KParams& p, CellIndex& ci)
    ci.dxp = (x == p.nx - 1) ? -(p.nx - 1) : 1;
    ci.dym = (y == 0) ? (p.ny - 1) * p.nx : -p.nx;
    ci.dyp = (y == p.ny - 1) ? -(p.ny - 1) * p.nx : p.nx;
-   const int64_t nxy = (int64_t)p.nx * p.ny;
-   ci.dzm = (z == 0) ? (int64_t)(p.nz - 1) * nxy : -nxy;
-   ci.dzp = (z == p.nz - 1) ? -(int64_t)(p.nz - 1) * nxy : nxy;
+   const int nxy = p.nx * p.ny;
+   ci.dzm = (z == 0) ? (p.nz - 1) * nxy : -nxy;
+   ci.dzp = (z == p.nz - 1) ? -(p.nz - 1) * nxy : nxy;
    return true;
 }
 
 // Cell index of x + (sx, sy, sz) with periodic wrap on every axis (a wrapped
 // neighbour across a non-periodic face is always flagged in the link word and
 // never dereferenced).
-__device__ __forceinline__ int64_t nbr(const CellIndex& ci, int sx, int sy, int sz)
+template <typename IT>
+__device__ __forceinline__ IT nbr(const CellIndex& ci, int sx, int sy, int sz)
 {
-   int64_t n = ci.c;
-   if (sx > 0) n += ci.dxp; else if (sx < 0) n += ci.dxm;
-   if (sy > 0) n += ci.dyp; else if (sy < 0) n += ci.dym;
-   if (sz > 0) n += ci.dzp; else if (sz < 0) n += ci.dzm;
-   return n;
+   int off = 0;
+   if (sx > 0) off += ci.dxp; else if (sx < 0) off += ci.dxm;
+   if (sy > 0) off += ci.dyp; else if (sy < 0) off += ci.dym;
+   if (sz > 0) off += ci.dzp; else if (sz < 0) off += ci.dzm;
+   return (IT)ci.c + (IT)off;
 }
 
 // Source (slot index) that direction s of this cell is read from.
-template <int Q, int KIND, bool LINKS>
-__device__ __forceinline__ int64_t read_index(const KParams& p, const CellIndex& ci, uint32_t lk, int s)
+template <int Q, int KIND, bool LINKS, typename IT>
+__device__ __forceinline__ IT read_index(const KParams& p, const CellIndex& ci, uint32_t lk, int s)
 {
    const int o = lat_opp(Q, s);
-   if (KIND == K_AA_EVEN) return (int64_t)o * p.plane + ci.c;
-   if (KIND == K_AB_PUSH || s == lat_rest(Q)) return (int64_t)s * p.plane + ci.c;
+   const IT plane = (IT)p.plane, c = (IT)ci.c;
+   if (KIND == K_AA_EVEN) return (IT)o * plane + c;
+   if (KIND == K_AB_PUSH || s == lat_rest(Q)) return (IT)s * plane + c;
    // AA odd, AB pull: slot s at x - c_s unless that neighbour is blocked.
-   if (LINKS && ((lk >> o) & 1u)) return (int64_t)o * p.plane + ci.c;
-   return (int64_t)s * p.plane + nbr(ci, -lat_c(Q, s, 0), -lat_c(Q, s, 1), -lat_c(Q, s, 2));
+   if (LINKS && ((lk >> o) & 1u)) return (IT)o * plane + c;
+   return (IT)s * plane + nbr<IT>(ci, -lat_c(Q, s, 0), -lat_c(Q, s, 1), -lat_c(Q, s, 2));
 }
 
 // Destination (slot index) of the post-collision value of direction s.
-template <int Q, int KIND, bool LINKS>
-__device__ __forceinline__ int64_t write_index(const KParams& p, const CellIndex& ci, uint32_t lk, int s)
+template <int Q, int KIND, bool LINKS, typename IT>
+__device__ __forceinline__ IT write_index(const KParams& p, const CellIndex& ci, uint32_t lk, int s)
 {
    const int o = lat_opp(Q, s);
-   if (KIND == K_AA_EVEN || KIND == K_AB_PULL || s == lat_rest(Q)) return (int64_t)s * p.plane + ci.c;
+   const IT plane = (IT)p.plane, c = (IT)ci.c;
+   if (KIND == K_AA_EVEN || KIND == K_AB_PULL || s == lat_rest(Q)) return (IT)s * plane + c;
    const bool blocked = LINKS && ((lk >> s) & 1u);
    if (KIND == K_AA_ODD) {
-      if (blocked) return (int64_t)s * p.plane + ci.c;
-      return (int64_t)o * p.plane + nbr(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+      if (blocked) return (IT)s * plane + c;
+      return (IT)o * plane + nbr<IT>(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
    }
    // AB push
-   if (blocked) return (int64_t)o * p.plane + ci.c;
-   return (int64_t)s * p.plane + nbr(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+   if (blocked) return (IT)o * plane + c;
+   return (IT)s * plane + nbr<IT>(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
 }
 
 template <bool FIELDS>
@@ -120,7 +125,7 @@ __device__ __forceinline__ void cell_force_f32(const KParams& p, int64_t c, floa
 }
 
 // One launch = one time step (or one range of it) of one propagation kind.
-template <int Q, int ST, int AR, int KIND, bool LINKS, bool FIELDS>
+template <int Q, int ST, int AR, int KIND, bool LINKS, bool FIELDS, typename IT>
 __global__ void __launch_bounds__(256) step_kernel(const KParams p, const typename Store<ST>::T* src,
                                                    typename Store<ST>::T* dst)
 {
@@ -134,31 +139,31 @@ __global__ void __launch_bounds__(256) step_kernel(const KParams p, const typena
    if constexpr (AR == AR_F64) {
       double d[Q], o[Q];
 #pragma unroll
-      for (int s = 0; s < Q; s++) d[s] = src[read_index<Q, KIND, LINKS>(p, ci, lk, s)];
+      for (int s = 0; s < Q; s++) d[s] = src[read_index<Q, KIND, LINKS, IT>(p, ci, lk, s)];
       double F0, F1, F2, sp;
       cell_force_f64<FIELDS>(p, ci.c, F0, F1, F2, sp);
       collide_f64<Q>(d, o, F0, F1, F2, sp, p);
 #pragma unroll
-      for (int s = 0; s < Q; s++) dst[write_index<Q, KIND, LINKS>(p, ci, lk, s)] = o[s];
+      for (int s = 0; s < Q; s++) dst[write_index<Q, KIND, LINKS, IT>(p, ci, lk, s)] = o[s];
    } else if constexpr (AR == AR_F64X) {
       uint64_t bits[Q];
       const unsigned long long* s64 = reinterpret_cast<const unsigned long long*>(src);
 #pragma unroll
-      for (int s = 0; s < Q; s++) bits[s] = s64[read_index<Q, KIND, LINKS>(p, ci, lk, s)];
+      for (int s = 0; s < Q; s++) bits[s] = s64[read_index<Q, KIND, LINKS, IT>(p, ci, lk, s)];
       static_assert(!FIELDS, "per-cell fields use the exact FP64 arithmetic");
       collide_f64x<Q>(bits, p);
       unsigned long long* d64 = reinterpret_cast<unsigned long long*>(dst);
 #pragma unroll
-      for (int s = 0; s < Q; s++) d64[write_index<Q, KIND, LINKS>(p, ci, lk, s)] = bits[s];
+      for (int s = 0; s < Q; s++) d64[write_index<Q, KIND, LINKS, IT>(p, ci, lk, s)] = bits[s];
    } else {
       float g[Q], o[Q];
 #pragma unroll
-      for (int s = 0; s < Q; s++) g[s] = load_shifted(src + read_index<Q, KIND, LINKS>(p, ci, lk, s));
+      for (int s = 0; s < Q; s++) g[s] = load_shifted(src + read_index<Q, KIND, LINKS, IT>(p, ci, lk, s));
       float F0, F1, F2, sp;
       cell_force_f32<FIELDS>(p, ci.c, F0, F1, F2, sp);
       collide_f32<Q>(g, o, F0, F1, F2, sp, p);
 #pragma unroll
-      for (int s = 0; s < Q; s++) store_shifted(dst + write_index<Q, KIND, LINKS>(p, ci, lk, s), o[s]);
+      for (int s = 0; s < Q; s++) store_shifted(dst + write_index<Q, KIND, LINKS, IT>(p, ci, lk, s), o[s]);
    }
 }
 

@@ -10,7 +10,13 @@ PATTERN_NAMES = {0: "aa", 1: "ab_push", 2: "ab_pull"}
 
 
 def golden_cases():
-    return sorted(p.stem for p in GOLDEN.glob("*.npz"))
+    """Box / channel cases (reference kernels on a harness geometry)."""
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("cylinder_"))
+
+
+def cylinder_cases():
+    """The reference's whole app flow on its cylinder (centre plane kept)."""
+    return sorted(p.stem for p in GOLDEN.glob("cylinder_*.npz"))
 
 
 def load_golden(name):

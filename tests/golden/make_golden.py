@@ -49,6 +49,34 @@ def case_inputs(Q, dims, walls, U, noise, seed=7):
     return f0, solid
 
 
+# Reference app flow (src/Main.cpp) on the cylinder, size 2: keys of the
+# reference's input files; only the centre x-plane of the readouts is kept.
+CYLINDER_CASES = {
+    "cylinder_s2_aa_unroll": dict(propPattern=1, pull=0, unroll=1),
+    "cylinder_s2_ab_push_unroll": dict(propPattern=0, pull=0, unroll=1),
+    "cylinder_s2_ab_pull_unroll": dict(propPattern=0, pull=1, unroll=1),
+}
+CYLINDER_STEPS = 100
+
+
+def cylinder_input(path, propPattern, pull, unroll, steps=CYLINDER_STEPS, size=2.0):
+    path.write_text(f"simulationSize {size}\npropPattern {propPattern}\npull {pull}\nunroll {unroll}\n"
+                    f"densityChange 0.01\nwritevtk 0\ntimesteps {steps}\n")
+    return path
+
+
+def make_cylinder(tmpdir):
+    for name, keys in CYLINDER_CASES.items():
+        inp = cylinder_input(Path(tmpdir) / f"{name}.txt", **keys)
+        out = ref.app_run(19, inp, omega=1.0, gx=1e-6)
+        nx = out["dims"][0]
+        cx = (nx - 1) // 2
+        np.savez_compressed(HERE / f"{name}.npz", dims=np.array(out["dims"]), nfluid=out["nfluid"],
+                            steps=out["steps"], centre_x=cx, rho_plane=out["rho"][:, :, cx],
+                            u_plane=out["u"][:, :, :, cx], f_plane=out["f_raw"][:, :, :, cx], **keys)
+        print(f"{name}: nfluid {out['nfluid']}")
+
+
 def main():
     if not ref.available():
         sys.exit("reference harness unavailable (oracle/build_ref.sh needs the reference sources)")
@@ -59,6 +87,9 @@ def main():
                             periodic=np.array(per), solid=solid, omega=1.0 / tau, gx=gx, steps=steps,
                             f_init=f0, f_raw=raw, variant=variant)
         print(f"{name}: {raw.nbytes + f0.nbytes} bytes")
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        make_cylinder(tmp)
 
 
 if __name__ == "__main__":
