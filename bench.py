@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--no-variants", action="store_true", help="skip the other storage formats")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--storage", default="f64", choices=["f64", "f32", "bf16", "f16"],
+                    help="population storage of the timed run (headline: f64)")
+    ap.add_argument("--lattice", type=int, default=19, choices=[19, 27])
+    ap.add_argument("--pattern", default="aa", choices=["aa", "ab_push", "ab_pull"])
     return ap.parse_args()
 
 
@@ -211,11 +215,13 @@ def main():
     torch.cuda.set_device(local)
     n = args.n
     ncell = n ** 3
-    Q = 19
-    bpu = 2 * Q * 8
+    Q = args.lattice
     u = workload_velocity(n)
-    sim = lbm.Simulation(n, n, n, lattice=Q, pattern="aa", omega=1.0 / TAU, force=(0, 0, 0), storage="f64",
-                         arithmetic="f64x", device=local)
+    arith = "f64x" if args.storage == "f64" else "auto"
+    sim = lbm.Simulation(n, n, n, lattice=Q, pattern=args.pattern, omega=1.0 / TAU, force=(0, 0, 0),
+                         storage=args.storage, arithmetic=arith, device=local)
+    bpu = int(sim.info.bytes_per_update)
+    headline = (args.storage, Q, args.pattern, n) == ("f64", 19, "aa", 512)
     sim.init_equilibrium(None, u)
     for _ in range(max(args.warmup, 3)):
         sim.step(1)
@@ -246,9 +252,9 @@ def main():
     avg_launch_s = statistics.mean(per_launch_ms) * 1e-3
     achieved = ncell * bpu / avg_launch_s / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic_per_launch(),
+                "frac": round(achieved / peak, 4), "traffic": traffic_per_launch() if headline else None,
                 "peak_kind": f"{peak_kind} copy bandwidth",
-                "kernel": "step_kernel<19,F64,F64X,AA_EVEN|AA_ODD> (one launch per step)",
+                "kernel": f"step_kernel<{Q},{args.storage},{arith},{args.pattern}> (one launch per step)",
                 "algorithmic_bytes_per_launch": ncell * bpu}
 
     # end to end through the C ABI, pinned host buffers
@@ -278,7 +284,7 @@ def main():
     del u
 
     variants = {}
-    if not args.no_variants:
+    if not args.no_variants and headline:
         uv = workload_velocity(n)
         for storage, arith, steps in [("f16", "auto", 12), ("bf16", "auto", 12), ("f32", "auto", 12),
                                       ("f64", "f64", 3)]:
@@ -314,13 +320,15 @@ def main():
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": round(total_ms / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 storage, df64 (FP32-pair) arithmetic",
+            "dtype": "f64 storage, df64 (FP32-pair) arithmetic" if arith == "f64x" else
+                     f"{args.storage} storage (f - w), f32 arithmetic",
             "data": "synthetic (seeded Taylor-Green + SplitMix64 noise)",
-            "config": {"workload": "D3Q19 BGK AA, 512^3 periodic box, tau=0.55, Taylor-Green U=0.05 + "
-                                   "uniform 1e-3 noise, FP64 storage",
-                       "lattice": "D3Q19", "propagation": "AA", "grid": [n, n, n], "tau": TAU,
-                       "storage": "f64", "arithmetic": "F64X (within 1e-10 of the reference)",
-                       "l2": "state 20.4 GB >> 129 MB L2 (no flush needed)",
+            "config": {"workload": f"D3Q{Q} BGK {args.pattern.upper()}, {n}^3 periodic box, tau=0.55, "
+                                   f"Taylor-Green U=0.05 + uniform 1e-3 noise, {args.storage.upper()} storage",
+                       "lattice": f"D3Q{Q}", "propagation": args.pattern, "grid": [n, n, n], "tau": TAU,
+                       "storage": args.storage,
+                       "arithmetic": "F64X (within 1e-10 of the reference)" if arith == "f64x" else "FP32 on f - w",
+                       "l2": f"state {ncell * bpu / 2 / 1e9:.1f} GB >> 129 MB L2 (no flush needed)",
                        "parallelism": "independent replica per GPU" if world > 1 else "1 GPU"},
             "gpu_launches": launches,
             "roofline": roofline,

@@ -174,7 +174,7 @@ KParams make_params(const lbm_handle* h, int64_t start, int64_t end, Launch& L)
    L.block = dim3(bx, 1, 1);
    L.grid = dim3((c.nx + bx - 1) / bx, c.ny, (unsigned)(z1 - z0));
    L.stream = h->stream;
-   L.idx32 = (uint64_t)h->plane * (uint64_t)h->Q < (1ull << 32);
+   L.idx32 = (uint64_t)h->plane * (uint64_t)h->elem < (1ull << 32);   // plane stride in bytes
    return p;
 }
 

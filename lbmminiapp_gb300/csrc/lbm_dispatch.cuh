@@ -12,7 +12,7 @@ namespace lbm {
 struct Launch {
    dim3 grid, block;
    cudaStream_t stream;
-   bool idx32;   // Q * plane < 2^32: 32-bit slot indices
+   bool idx32;   // plane stride below 2^32 bytes: 32-bit stride arithmetic
 };
 
 template <int Q, int ST, int AR, int KIND>
@@ -24,9 +24,8 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
    T* d = static_cast<T*>(dst);
    // Per-cell fields always use the exact FP64 arithmetic when FP64 is stored.
    constexpr int ARF = (AR == AR_F64X) ? AR_F64 : AR;
-   // Per-cell fields (porosity, force field) are the adjoint / research
-   // configurations: 64-bit indices only.  The plain step kernels get a 32-bit
-   // index variant for buffers of fewer than 2^32 elements.
+   // Per-cell fields (porosity, force field): 64-bit stride arithmetic only.
+   // The plain step kernels get a 32-bit stride variant for planes below 4 GiB.
    if (fields) {
       if (links) step_kernel<Q, ST, ARF, KIND, true, true, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
       else step_kernel<Q, ST, ARF, KIND, false, true, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);

@@ -204,24 +204,27 @@ __host__ __device__ __forceinline__ df df_from_double(double d)
 }
 
 // ------------------------------------------------ double <-> float pair
-// Fast-path range of the double bit patterns: positive, 2^-80 <= f < 1.
-constexpr uint32_t kHiMin = (uint32_t)(1023 - 80) << 20;   // high word of 2^-80
+// Fast-path range of the double bit patterns: positive, 2^-75 <= f < 1.
+constexpr uint32_t kHiMin = (uint32_t)(1023 - 75) << 20;   // high word of 2^-75
 constexpr uint32_t kHiMax = (uint32_t)1023 << 20;          // high word of 1.0 (excluded)
 
 // Split a double (given as its 64-bit pattern, in range) into (h, l).
 //   t  = bits 59..28 of the pattern: the low 8 exponent bits above the top
 //        23 mantissa bits; adding 2^30 re-biases exponent 1023 to 127
 //        (E - 896) within the 8-bit field, valid for E in [897, 1150].
-//   l  = next 23 mantissa bits, built as a float with exponent e(h) - 23 and
-//        its implicit 1 subtracted (exact by Sterbenz).
+//   l  = the remaining 29 mantissa bits rounded to nearest 23 (a float with
+//        exponent e(h) - 23 and its implicit 1 subtracted, exact by Sterbenz;
+//        a carry out of the 23 bits moves into that float's exponent, which
+//        is still the correctly rounded value).  |f - (h + l)| <= 2^-48 |f|.
 __host__ __device__ __forceinline__ df split(uint64_t bits)
 {
    const uint32_t lo = (uint32_t)bits, hi = (uint32_t)(bits >> 32);
    const uint32_t t = funnel_l(lo, hi, 3);
    const uint32_t hb = ((t + 0x40000000u) & 0x7FFFFFFFu) | (hi & 0x80000000u);
    const uint32_t a = hb - (23u << 23);
-   const uint32_t xb = (a & 0xFF800000u) | ((lo >> 6) & 0x007FFFFFu);
    const uint32_t mb = a & 0xFF800000u;
+   const uint32_t m24 = (lo >> 5) & 0x00FFFFFFu;          // 23 bits + the rounding bit
+   const uint32_t xb = mb + ((m24 + 1u) >> 1);             // round half up
    return {bitsf(hb), fsub(bitsf(xb), bitsf(mb))};
 }
 
@@ -242,19 +245,32 @@ __host__ __device__ __forceinline__ uint64_t join(df v)
    return d0 + (uint64_t)((int64_t)ei * 128);
 }
 
-// join() plus the output range check on S, the float rounding of the result:
-// ok becomes false unless 2^-80 <= S < 1 (positive, inside the fast range).
+__host__ __device__ __forceinline__ int32_t f2i_rn(float x)
+{
+#ifdef __CUDA_ARCH__
+   return __float2int_rn(x);
+#else
+   return (int32_t)std::nearbyint(x);
+#endif
+}
+
+// Double pattern of h + l (positive) with the output range check folded in:
+//   S  = h + l rounded toward zero (so the remainder E >= 0 stays inside S's
+//        binade), E = the remainder (exact);
+//   N  = E in units of one double ulp of S, an exact float below 2^29,
+//        rounded to the nearest integer;
+//   the pattern of S as a double plus N: the double nearest to h + l.
+// ok becomes false unless 2^-75 <= S < 1.
 __host__ __device__ __forceinline__ uint64_t join_checked(df v, bool& ok)
 {
    const float S = fadd_rz(v.h, v.l);
    const float E = fsub(v.l, fsub(S, v.h));
    const uint32_t sb = fbits(S);
-   ok = ok && (sb - 0x17800000u) < (0x3F800000u - 0x17800000u);
-   const float scale = bitsf(0x95800000u - (sb & 0x7F800000u));  // 2^(45 - e(S))
-   const float y = ffma(E, scale, 12582912.0f);
-   const int32_t ei = (int32_t)(fbits(y) - 0x4B400000u);
+   ok = ok && (sb - 0x1A000000u) < (0x3F800000u - 0x1A000000u);
+   const float scale = bitsf(0x99000000u - (sb & 0x7F800000u));  // 2^(52 - e(S))
+   const int32_t n = f2i_rn(fmul(E, scale));
    const uint64_t d0 = ((uint64_t)sb << 29) + ((uint64_t)0x38000000u << 32);
-   return d0 + (uint64_t)((int64_t)ei * 128);
+   return d0 + (uint64_t)(int64_t)n;
 }
 
 __host__ __device__ __forceinline__ bool in_range(uint64_t bits)
@@ -327,12 +343,12 @@ constexpr uint32_t kHiQuarter = (uint32_t)(1023 - 2) << 20;   // 0.25
 // The fast-path collision on one cell.  bits[] holds the Q input patterns in
 // direction order and receives the Q output patterns.  Returns false (leaving
 // bits[] untouched) when the cell must take the exact path:
-//   * inputs: rest population in [0.25, 1), the others in [2^-80, 0.25) --
-//     so rho's running sum, started at the rest population, always has an
+//   * inputs: rest population in [0.25, 1), the others in [2^-75, 0.25) --
+//     (and 2^-75 below) so rho's running sum, started at the rest population, always has an
 //     exponent at least that of the next term (Fast2Sum is exact);
 //   * |3 v_d| < 0.3: |c.u| stays well below 1 - uu/2, so the pair sums
 //     (1 - uu/2 + cu^2/2) +- cu keep their larger operand first;
-//   * outputs inside [2^-80, 1).
+//   * outputs inside [2^-75, 1).
 // Work is organised by opposite pairs (s, opp(s)): cu, the quadratic term and
 // the omega*w*rho products are shared, since cu(opp) = -cu(s).
 template <int Q, bool FORCE>

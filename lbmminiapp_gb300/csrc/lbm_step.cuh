@@ -24,9 +24,9 @@
 
 namespace lbm {
 
-// Cell and slot indices: IT is uint32_t when Q * plane < 2^32 (one IMAD per
-// slot index, one IMAD.WIDE per address), int64_t otherwise.  Cell indices and
-// neighbour offsets always fit 32 bits (fewer than 2^31 cells per handle).
+// IT is uint32_t when a plane is below 4 GiB (32-bit stride arithmetic),
+// int64_t otherwise.  Cell indices and neighbour offsets always fit 32 bits
+// (fewer than 2^31 cells per handle).
 struct CellIndex {
    int64_t c;
    int dxm, dxp, dym, dyp, dzm, dzp;   // neighbour offsets in cells
@@ -54,44 +54,55 @@ __device__ __forceinline__ bool cell_of_thread(const KParams& p, CellIndex& ci)
 // Cell index of x + (sx, sy, sz) with periodic wrap on every axis (a wrapped
 // neighbour across a non-periodic face is always flagged in the link word and
 // never dereferenced).
-template <typename IT>
-__device__ __forceinline__ IT nbr(const CellIndex& ci, int sx, int sy, int sz)
+__device__ __forceinline__ int nbr_off(const CellIndex& ci, int sx, int sy, int sz)
 {
    int off = 0;
    if (sx > 0) off += ci.dxp; else if (sx < 0) off += ci.dxm;
    if (sy > 0) off += ci.dyp; else if (sy < 0) off += ci.dym;
    if (sz > 0) off += ci.dzp; else if (sz < 0) off += ci.dzm;
-   return (IT)ci.c + (IT)off;
+   return off;
 }
 
-// Source (slot index) that direction s of this cell is read from.
-template <int Q, int KIND, bool LINKS, typename IT>
-__device__ __forceinline__ IT read_index(const KParams& p, const CellIndex& ci, uint32_t lk, int s)
+// Access to slot `slot` of the cell at offset `off` (in cells, small and
+// signed) from this thread's cell: byte address = cell base + slot * plane
+// bytes + off * element bytes.  With IT = uint32_t the plane stride in bytes
+// fits 32 bits and slot * stride is one 32x32->64 multiply-add.
+struct Access {
+   int slot;
+   int off;
+};
+
+template <int Q, int KIND, bool LINKS>
+__device__ __forceinline__ Access read_access(const CellIndex& ci, uint32_t lk, int s)
 {
    const int o = lat_opp(Q, s);
-   const IT plane = (IT)p.plane, c = (IT)ci.c;
-   if (KIND == K_AA_EVEN) return (IT)o * plane + c;
-   if (KIND == K_AB_PUSH || s == lat_rest(Q)) return (IT)s * plane + c;
+   if (KIND == K_AA_EVEN) return {o, 0};
+   if (KIND == K_AB_PUSH || s == lat_rest(Q)) return {s, 0};
    // AA odd, AB pull: slot s at x - c_s unless that neighbour is blocked.
-   if (LINKS && ((lk >> o) & 1u)) return (IT)o * plane + c;
-   return (IT)s * plane + nbr<IT>(ci, -lat_c(Q, s, 0), -lat_c(Q, s, 1), -lat_c(Q, s, 2));
+   if (LINKS && ((lk >> o) & 1u)) return {o, 0};
+   return {s, nbr_off(ci, -lat_c(Q, s, 0), -lat_c(Q, s, 1), -lat_c(Q, s, 2))};
 }
 
-// Destination (slot index) of the post-collision value of direction s.
-template <int Q, int KIND, bool LINKS, typename IT>
-__device__ __forceinline__ IT write_index(const KParams& p, const CellIndex& ci, uint32_t lk, int s)
+template <int Q, int KIND, bool LINKS>
+__device__ __forceinline__ Access write_access(const CellIndex& ci, uint32_t lk, int s)
 {
    const int o = lat_opp(Q, s);
-   const IT plane = (IT)p.plane, c = (IT)ci.c;
-   if (KIND == K_AA_EVEN || KIND == K_AB_PULL || s == lat_rest(Q)) return (IT)s * plane + c;
+   if (KIND == K_AA_EVEN || KIND == K_AB_PULL || s == lat_rest(Q)) return {s, 0};
    const bool blocked = LINKS && ((lk >> s) & 1u);
    if (KIND == K_AA_ODD) {
-      if (blocked) return (IT)s * plane + c;
-      return (IT)o * plane + nbr<IT>(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+      if (blocked) return {s, 0};
+      return {o, nbr_off(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2))};
    }
    // AB push
-   if (blocked) return (IT)o * plane + c;
-   return (IT)s * plane + nbr<IT>(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+   if (blocked) return {o, 0};
+   return {s, nbr_off(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2))};
+}
+
+template <typename T, typename IT>
+__device__ __forceinline__ T* slot_ptr(T* cell_base, IT plane_bytes, Access a)
+{
+   const uintptr_t p = reinterpret_cast<uintptr_t>(cell_base) + (uint64_t)(uint32_t)a.slot * (uint64_t)plane_bytes;
+   return reinterpret_cast<T*>(p) + a.off;
 }
 
 template <bool FIELDS>
@@ -136,34 +147,38 @@ __global__ void __launch_bounds__(256) step_kernel(const KParams p, const typena
       lk = p.links[ci.c];
       if (lk & kSolidBit) return;
    }
+   using T = typename Store<ST>::T;
+   const IT pb = (IT)p.plane * (IT)sizeof(T);
+   const T* sbase = src + ci.c;
+   T* dbase = dst + ci.c;
    if constexpr (AR == AR_F64) {
       double d[Q], o[Q];
 #pragma unroll
-      for (int s = 0; s < Q; s++) d[s] = src[read_index<Q, KIND, LINKS, IT>(p, ci, lk, s)];
+      for (int s = 0; s < Q; s++) d[s] = *slot_ptr(sbase, pb, read_access<Q, KIND, LINKS>(ci, lk, s));
       double F0, F1, F2, sp;
       cell_force_f64<FIELDS>(p, ci.c, F0, F1, F2, sp);
       collide_f64<Q>(d, o, F0, F1, F2, sp, p);
 #pragma unroll
-      for (int s = 0; s < Q; s++) dst[write_index<Q, KIND, LINKS, IT>(p, ci, lk, s)] = o[s];
+      for (int s = 0; s < Q; s++) *slot_ptr(dbase, pb, write_access<Q, KIND, LINKS>(ci, lk, s)) = o[s];
    } else if constexpr (AR == AR_F64X) {
       uint64_t bits[Q];
-      const unsigned long long* s64 = reinterpret_cast<const unsigned long long*>(src);
+      const unsigned long long* s64 = reinterpret_cast<const unsigned long long*>(sbase);
 #pragma unroll
-      for (int s = 0; s < Q; s++) bits[s] = s64[read_index<Q, KIND, LINKS, IT>(p, ci, lk, s)];
+      for (int s = 0; s < Q; s++) bits[s] = *slot_ptr(s64, pb, read_access<Q, KIND, LINKS>(ci, lk, s));
       static_assert(!FIELDS, "per-cell fields use the exact FP64 arithmetic");
       collide_f64x<Q>(bits, p);
-      unsigned long long* d64 = reinterpret_cast<unsigned long long*>(dst);
+      unsigned long long* d64 = reinterpret_cast<unsigned long long*>(dbase);
 #pragma unroll
-      for (int s = 0; s < Q; s++) d64[write_index<Q, KIND, LINKS, IT>(p, ci, lk, s)] = bits[s];
+      for (int s = 0; s < Q; s++) *slot_ptr(d64, pb, write_access<Q, KIND, LINKS>(ci, lk, s)) = bits[s];
    } else {
       float g[Q], o[Q];
 #pragma unroll
-      for (int s = 0; s < Q; s++) g[s] = load_shifted(src + read_index<Q, KIND, LINKS, IT>(p, ci, lk, s));
+      for (int s = 0; s < Q; s++) g[s] = load_shifted(slot_ptr(sbase, pb, read_access<Q, KIND, LINKS>(ci, lk, s)));
       float F0, F1, F2, sp;
       cell_force_f32<FIELDS>(p, ci.c, F0, F1, F2, sp);
       collide_f32<Q>(g, o, F0, F1, F2, sp, p);
 #pragma unroll
-      for (int s = 0; s < Q; s++) store_shifted(dst + write_index<Q, KIND, LINKS, IT>(p, ci, lk, s), o[s]);
+      for (int s = 0; s < Q; s++) store_shifted(slot_ptr(dbase, pb, write_access<Q, KIND, LINKS>(ci, lk, s)), o[s]);
    }
 }
 
