@@ -175,6 +175,11 @@ KParams make_params(const lbm_handle* h, int64_t start, int64_t end, Launch& L)
    L.grid = dim3((c.nx + bx - 1) / bx, c.ny, (unsigned)(z1 - z0));
    L.stream = h->stream;
    L.idx32 = (uint64_t)h->plane * (uint64_t)h->elem < (1ull << 32);   // plane stride in bytes
+   L.pair = h->storage != ST_F64 && c.nx % 2 == 0 && start == 0 && end == h->ncell;
+   const int half = c.nx / 2;
+   const int pbx = (int)std::min<int64_t>(256, ((half + 31) / 32) * 32);
+   L.pair_block = dim3(pbx, 1, 1);
+   L.pair_grid = dim3((half + pbx - 1) / pbx, c.ny, (unsigned)(z1 - z0));
    return p;
 }
 

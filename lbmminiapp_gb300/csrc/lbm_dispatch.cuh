@@ -13,6 +13,8 @@ struct Launch {
    dim3 grid, block;
    cudaStream_t stream;
    bool idx32;   // plane stride below 2^32 bytes: 32-bit stride arithmetic
+   bool pair;    // two cells per thread (shifted storage, periodic box, even nx, full grid)
+   dim3 pair_grid, pair_block;
 };
 
 template <int Q, int ST, int AR, int KIND>
@@ -22,6 +24,13 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
    using T = typename Store<ST>::T;
    const T* s = static_cast<const T*>(src);
    T* d = static_cast<T*>(dst);
+   if constexpr (ST != ST_F64) {
+      if (L.pair && !links && !fields) {
+         if (L.idx32) step_pair_kernel<Q, ST, KIND, uint32_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
+         else step_pair_kernel<Q, ST, KIND, int64_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
+         return cudaGetLastError();
+      }
+   }
    // Per-cell fields always use the exact FP64 arithmetic when FP64 is stored.
    constexpr int ARF = (AR == AR_F64X) ? AR_F64 : AR;
    // Per-cell fields (porosity, force field): 64-bit stride arithmetic only.

@@ -151,43 +151,122 @@ __device__ __forceinline__ void collide_f64(double (&d)[Q], double (&o)[Q], doub
 }
 
 // ------------------------------------------- FP32 shifted collision
-// g = f - w.  With drho = sum g (sum w = 1) and j = sum c g (sum c w = 0):
+// Stored values are G = S (f - w) with S = 2^15 for FP16 and 1 otherwise.
+// With drho = sum (f - w) (sum w = 1) and j = sum c (f - w) (sum c w = 0):
 //   eq_s - w_s = w_s (drho + rho (cu + cu^2/2 - uu/2))
-//   g_s'       = (1-omega) g_s + omega (eq_s - w_s) + (1-omega/2) fdist_s
-// which keeps the large constant w out of the single-precision arithmetic.
-template <int Q>
-__device__ __forceinline__ void collide_f32(float (&g)[Q], float (&o)[Q], float F0, float F1, float F2,
+//   G_s'       = (1-omega) G_s + omega S (eq_s - w_s) + (1-omega/2) S fdist_s
+// which keeps the large constant w out of the single-precision arithmetic;
+// S enters only through per-cell factors.  Opposite directions share
+// cu(opp) = -cu, so S (eq - w) = A +- B with A = w (S drho + S rho (cu^2 - uu)/2)
+// and B = w S rho cu.
+template <int ST> struct ShiftScale { static constexpr float S = 1.0f; };
+template <> struct ShiftScale<ST_F16> { static constexpr float S = kF16Scale; };
+
+__device__ __forceinline__ float load_raw(const float* p) { return *p; }
+__device__ __forceinline__ float load_raw(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+__device__ __forceinline__ float load_raw(const __half* p) { return __half2float(*p); }
+__device__ __forceinline__ void store_raw(float* p, float g) { *p = g; }
+__device__ __forceinline__ void store_raw(__nv_bfloat16* p, float g) { *p = __float2bfloat16_rn(g); }
+__device__ __forceinline__ void store_raw(__half* p, float g) { *p = __float2half_rn(g); }
+
+template <int Q, int S_>
+__device__ __forceinline__ float cdot_f(const float (&v)[3])
+{
+   constexpr int c0 = lat_c(Q, S_, 0), c1 = lat_c(Q, S_, 1), c2 = lat_c(Q, S_, 2);
+   float r = 0.0f;
+   bool any = false;
+   if (c0 != 0) { r = c0 > 0 ? v[0] : -v[0]; any = true; }
+   if (c1 != 0) { r = any ? (c1 > 0 ? r + v[1] : r - v[1]) : (c1 > 0 ? v[1] : -v[1]); any = true; }
+   if (c2 != 0) { r = any ? (c2 > 0 ? r + v[2] : r - v[2]) : (c2 > 0 ? v[2] : -v[2]); }
+   return r;
+}
+
+template <int Q, int ST, bool FORCE, int P = 0>
+__device__ __forceinline__ void collide_pairs_f32(const float (&G)[Q], float (&o)[Q], const float (&u3)[3],
+                                                  const float (&F3)[3], float fu, float uu, const float (&wSd)[4],
+                                                  const float (&wSr)[4], float om1, float omega, float Som2,
+                                                  int compat)
+{
+   if constexpr (P < (Q - 1) / 2) {
+      // representative s < opp(s) of the P-th pair
+      constexpr int s = [] {
+         int seen = 0;
+         for (int t = 0; t < Q; t++)
+            if (t < lat_opp(Q, t)) {
+               if (seen == P) return t;
+               seen++;
+            }
+         return -1;
+      }();
+      constexpr int ob = lat_opp(Q, s);
+      constexpr int cls = lat_norm2(Q, s);
+      const float cu = cdot_f<Q, s>(u3);
+      const float A = fmaf(wSr[cls], 0.5f * fmaf(cu, cu, -uu), wSd[cls]);
+      const float B = wSr[cls] * cu;
+      float fs = 0.0f, fo = 0.0f;
+      if (FORCE) {
+         constexpr float w = (float)lat_w(Q, s);
+         const float cf = cdot_f<Q, s>(F3);
+         const float sym = fmaf(cu, cf, -fu);
+         fs = Som2 * w * (cf + sym);
+         fo = Som2 * w * (sym - cf);
+      }
+      o[s] = fmaf(om1, G[s], fmaf(omega, A + B, fs));
+      o[ob] = fmaf(om1, G[ob], fmaf(omega, A - B, fo));
+      collide_pairs_f32<Q, ST, FORCE, P + 1>(G, o, u3, F3, fu, uu, wSd, wSr, om1, omega, Som2, compat);
+   }
+}
+
+template <int Q, int ST, bool FORCE>
+__device__ __forceinline__ void collide_f32(const float (&G)[Q], float (&o)[Q], float F0, float F1, float F2,
                                             float sp, const KParams& p)
 {
-   float drho = 0.f, j0 = 0.f, j1 = 0.f, j2 = 0.f;
+   constexpr float S = ShiftScale<ST>::S;
+   constexpr float iS = 1.0f / S;
+   float Sd = 0.f, j0 = 0.f, j1 = 0.f, j2 = 0.f;
 #pragma unroll
    for (int s = 0; s < Q; s++) {
-      drho += g[s];
+      Sd += G[s];
       const int c0 = lat_c(Q, s, 0), c1 = lat_c(Q, s, 1), c2 = lat_c(Q, s, 2);
-      if (c0 > 0) j0 += g[s]; else if (c0 < 0) j0 -= g[s];
-      if (c1 > 0) j1 += g[s]; else if (c1 < 0) j1 -= g[s];
-      if (c2 > 0) j2 += g[s]; else if (c2 < 0) j2 -= g[s];
+      if (c0 > 0) j0 += G[s]; else if (c0 < 0) j0 -= G[s];
+      if (c1 > 0) j1 += G[s]; else if (c1 < 0) j1 -= G[s];
+      if (c2 > 0) j2 += G[s]; else if (c2 < 0) j2 -= G[s];
    }
-   const float rho = 1.0f + drho;
+   const float rho = fmaf(Sd, iS, 1.0f);
    const float ir = __frcp_rn(rho);
-   const float u0 = (j0 + 0.5f * F0) * ir, u1 = (j1 + 0.5f * F1) * ir, u2 = (j2 + 0.5f * F2) * ir;
-   const float uu = 3.0f * (u0 * u0 + u1 * u1 + u2 * u2);
-   const float fu = 3.0f * (F0 * u0 + F1 * u1 + F2 * u2);
+   // 3u and 3F
+   const float ir3 = 3.0f * ir;
+   float u3[3] = {fmaf(j0, iS, 0.5f * F0) * ir3, fmaf(j1, iS, 0.5f * F1) * ir3, fmaf(j2, iS, 0.5f * F2) * ir3};
+   const float uu = (u3[0] * u3[0] + u3[1] * u3[1] + u3[2] * u3[2]) * (1.0f / 3.0f);   // 3 u.u
+   float F3[3] = {3.0f * F0, 3.0f * F1, 3.0f * F2};
+   const float fu = FORCE ? (F3[0] * u3[0] + F3[1] * u3[1] + F3[2] * u3[2]) * (1.0f / 3.0f) : 0.0f;
+   const float Sr = S * rho;
+   float wSd[4], wSr[4];
 #pragma unroll
-   for (int s = 0; s < Q; s++) {
-      const float c0 = (float)lat_c(Q, s, 0), c1 = (float)lat_c(Q, s, 1), c2 = (float)lat_c(Q, s, 2);
-      const float cu = 3.0f * (c0 * u0 + c1 * u1 + c2 * u2);
-      const float cf = 3.0f * (c0 * F0 + c1 * F1 + c2 * F2);
-      const float w = (float)lat_w(Q, s);
-      const float wf = (Q == 19 && s == lat_rest(Q) && p.compat) ? (float)(1.0 / 36.0) : w;
-      const float eqm = w * (drho + rho * (cu + 0.5f * cu * cu - 0.5f * uu));
-      const float fd = wf * (cf - fu + cu * cf);
-      o[s] = p.om1f * g[s] + p.omegaf * eqm + p.om2f * fd;
+   for (int c = 0; c < 4; c++) {
+      float w;
+      if (Q == 19) w = c == 0 ? (float)(1.0 / 3.0) : (c == 1 ? (float)(1.0 / 18.0) : (float)(1.0 / 36.0));
+      else w = c == 0 ? (float)(8.0 / 27.0) : (c == 1 ? (float)(2.0 / 27.0) : (c == 2 ? (float)(1.0 / 54.0) : (float)(1.0 / 216.0)));
+      wSd[c] = w * Sd;
+      wSr[c] = w * Sr;
+   }
+   const float Som2 = S * p.om2f;
+   collide_pairs_f32<Q, ST, FORCE>(G, o, u3, F3, fu, uu, wSd, wSr, p.om1f, p.omegaf, Som2, p.compat);
+   // rest: A = w (S drho + S rho (-uu/2)), forcing -wf fu
+   constexpr int R = lat_rest(Q);
+   {
+      const float A = fmaf(wSr[0], -0.5f * uu, wSd[0]);
+      float fr = 0.0f;
+      if (FORCE) {
+         const float wf = (Q == 19 && p.compat) ? (float)(1.0 / 36.0) : (float)lat_w(Q, R);
+         fr = -Som2 * wf * fu;
+      }
+      o[R] = fmaf(p.om1f, G[R], fmaf(p.omegaf, A, fr));
    }
    if (sp != 0.0f) {
       const float keep = 1.0f - sp;
 #pragma unroll
-      for (int s = 0; s < Q; s++) o[s] = keep * o[s] + sp * g[lat_opp(Q, s)];
+      for (int s = 0; s < Q; s++) o[s] = keep * o[s] + sp * G[lat_opp(Q, s)];
    }
 }
 

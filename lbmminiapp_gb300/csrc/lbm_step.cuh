@@ -173,12 +173,110 @@ __global__ void __launch_bounds__(256) step_kernel(const KParams p, const typena
    } else {
       float g[Q], o[Q];
 #pragma unroll
-      for (int s = 0; s < Q; s++) g[s] = load_shifted(slot_ptr(sbase, pb, read_access<Q, KIND, LINKS>(ci, lk, s)));
+      for (int s = 0; s < Q; s++) g[s] = load_raw(slot_ptr(sbase, pb, read_access<Q, KIND, LINKS>(ci, lk, s)));
       float F0, F1, F2, sp;
       cell_force_f32<FIELDS>(p, ci.c, F0, F1, F2, sp);
-      collide_f32<Q>(g, o, F0, F1, F2, sp, p);
+      if (FIELDS || p.forced) collide_f32<Q, ST, true>(g, o, F0, F1, F2, sp, p);
+      else collide_f32<Q, ST, false>(g, o, F0, F1, F2, sp, p);
 #pragma unroll
-      for (int s = 0; s < Q; s++) store_shifted(slot_ptr(dbase, pb, write_access<Q, KIND, LINKS>(ci, lk, s)), o[s]);
+      for (int s = 0; s < Q; s++) store_raw(slot_ptr(dbase, pb, write_access<Q, KIND, LINKS>(ci, lk, s)), o[s]);
+   }
+}
+
+// ------------------------------------------------------------------------
+// Two cells per thread (x0, x0+1) for shifted FP32/BF16/FP16 storage in a
+// fully periodic box: planes not shifted along x are read and written as one
+// aligned 2-element vector (half2 / bfloat162 / float2); x-shifted planes use
+// two scalar accesses.  Requires an even nx and a full-grid launch.
+template <typename T> struct PairVec;
+template <> struct PairVec<float> {
+   using V = float2;
+   __device__ static float2 get(V v) { return v; }
+   __device__ static V put(float a, float b) { return make_float2(a, b); }
+};
+template <> struct PairVec<__half> {
+   using V = __half2;
+   __device__ static float2 get(V v) { return __half22float2(v); }
+   __device__ static V put(float a, float b) { return __floats2half2_rn(a, b); }
+};
+template <> struct PairVec<__nv_bfloat16> {
+   using V = __nv_bfloat162;
+   __device__ static float2 get(V v) { return __bfloat1622float2(v); }
+   __device__ static V put(float a, float b) { return __floats2bfloat162_rn(a, b); }
+};
+
+__device__ __forceinline__ void cell_offsets(const KParams& p, int x, int y, int z, CellIndex& ci)
+{
+   ci.c = ((int64_t)z * p.ny + y) * p.nx + x;
+   ci.dxm = (x == 0) ? p.nx - 1 : -1;
+   ci.dxp = (x == p.nx - 1) ? -(p.nx - 1) : 1;
+   ci.dym = (y == 0) ? (p.ny - 1) * p.nx : -p.nx;
+   ci.dyp = (y == p.ny - 1) ? -(p.ny - 1) * p.nx : p.nx;
+   const int nxy = p.nx * p.ny;
+   ci.dzm = (z == 0) ? (p.nz - 1) * nxy : -nxy;
+   ci.dzp = (z == p.nz - 1) ? -(p.nz - 1) * nxy : nxy;
+}
+
+template <int Q, int KIND>
+__device__ constexpr bool read_shifted_x(int s)
+{
+   return (KIND == K_AA_ODD || KIND == K_AB_PULL) && s != lat_rest(Q) && lat_c(Q, s, 0) != 0;
+}
+
+template <int Q, int KIND>
+__device__ constexpr bool write_shifted_x(int s)
+{
+   return (KIND == K_AA_ODD || KIND == K_AB_PUSH) && s != lat_rest(Q) && lat_c(Q, s, 0) != 0;
+}
+
+template <int Q, int ST, int KIND, typename IT>
+__global__ void __launch_bounds__(256) step_pair_kernel(const KParams p, const typename Store<ST>::T* src,
+                                                        typename Store<ST>::T* dst)
+{
+   using T = typename Store<ST>::T;
+   using PV = PairVec<T>;
+   const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+   if (x0 >= p.nx) return;
+   const int y = blockIdx.y, z = p.z0 + blockIdx.z;
+   CellIndex c0, c1;
+   cell_offsets(p, x0, y, z, c0);
+   cell_offsets(p, x0 + 1, y, z, c1);
+   const IT pb = (IT)p.plane * (IT)sizeof(T);
+   const T* s0 = src + c0.c;
+   const T* s1 = src + c1.c;
+   T* d0 = dst + c0.c;
+   T* d1 = dst + c1.c;
+   float g0[Q], g1[Q], o0[Q], o1[Q];
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      const Access a0 = read_access<Q, KIND, false>(c0, 0u, s);
+      if (read_shifted_x<Q, KIND>(s)) {
+         const Access a1 = read_access<Q, KIND, false>(c1, 0u, s);
+         g0[s] = load_raw(slot_ptr(s0, pb, a0));
+         g1[s] = load_raw(slot_ptr(s1, pb, a1));
+      } else {
+         const float2 v = PV::get(*reinterpret_cast<const typename PV::V*>(slot_ptr(s0, pb, a0)));
+         g0[s] = v.x;
+         g1[s] = v.y;
+      }
+   }
+   if (p.forced) {
+      collide_f32<Q, ST, true>(g0, o0, p.Ff[0], p.Ff[1], p.Ff[2], 0.0f, p);
+      collide_f32<Q, ST, true>(g1, o1, p.Ff[0], p.Ff[1], p.Ff[2], 0.0f, p);
+   } else {
+      collide_f32<Q, ST, false>(g0, o0, 0.0f, 0.0f, 0.0f, 0.0f, p);
+      collide_f32<Q, ST, false>(g1, o1, 0.0f, 0.0f, 0.0f, 0.0f, p);
+   }
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      const Access a0 = write_access<Q, KIND, false>(c0, 0u, s);
+      if (write_shifted_x<Q, KIND>(s)) {
+         const Access a1 = write_access<Q, KIND, false>(c1, 0u, s);
+         store_raw(slot_ptr(d0, pb, a0), o0[s]);
+         store_raw(slot_ptr(d1, pb, a1), o1[s]);
+      } else {
+         *reinterpret_cast<typename PV::V*>(slot_ptr(d0, pb, a0)) = PV::put(o0[s], o1[s]);
+      }
    }
 }
 
