@@ -56,6 +56,8 @@ def parse():
                     help="population storage of the timed run (headline: f64)")
     ap.add_argument("--lattice", type=int, default=19, choices=[19, 27])
     ap.add_argument("--pattern", default="aa", choices=["aa", "ab_push", "ab_pull"])
+    ap.add_argument("--accuracy", action="store_true",
+                    help="print the mixed-precision error table (n^3, 1000 steps) instead of timing")
     return ap.parse_args()
 
 
@@ -212,6 +214,15 @@ def main():
     import torch
     import lbmminiapp_gb300 as lbm
 
+    if args.accuracy:
+        from lbmminiapp_gb300.accuracy import error_table
+        t0 = time.perf_counter()
+        table = error_table(n=args.n, steps=1000, tau=TAU, device=local)
+        print(json.dumps({"accuracy": table, "grid": [args.n] * 3, "steps": 1000, "tau": TAU,
+                          "workload": "D3Q19 AA Taylor-Green U=0.05 + 1e-3 noise, errors vs FP64 storage",
+                          "seconds": round(time.perf_counter() - t0, 1)}), flush=True)
+        return 0
+
     torch.cuda.set_device(local)
     n = args.n
     ncell = n ** 3
@@ -286,10 +297,10 @@ def main():
     variants = {}
     if not args.no_variants and headline:
         uv = workload_velocity(n)
-        for storage, arith, steps in [("f16", "auto", 12), ("bf16", "auto", 12), ("f32", "auto", 12),
-                                      ("f64", "f64", 3)]:
+        for storage, v_arith, steps in [("f16", "auto", 12), ("bf16", "auto", 12), ("f32", "auto", 12),
+                                        ("f64", "f64", 3)]:
             s2 = lbm.Simulation(n, n, n, lattice=Q, pattern="aa", omega=1.0 / TAU, force=(0, 0, 0),
-                                storage=storage, arithmetic=arith, device=local)
+                                storage=storage, arithmetic=v_arith, device=local)
             s2.init_equilibrium(None, uv)
             s2.step(2)
             torch.cuda.synchronize()
@@ -300,7 +311,7 @@ def main():
             b.synchronize()
             ms = a.elapsed_time(b) / steps
             bytes_u = s2.info.bytes_per_update
-            variants[f"{storage}/{arith}"] = {"MLUPS": round(ncell / (ms * 1e-3) / 1e6, 1),
+            variants[f"{storage}/{v_arith}"] = {"MLUPS": round(ncell / (ms * 1e-3) / 1e6, 1),
                                               "GB/s": round(ncell * bytes_u / (ms * 1e-3) / 1e9, 1),
                                               "bytes_per_update": bytes_u}
             s2.close()
