@@ -173,6 +173,34 @@ lbm_status lbm_timestep_force(lbm_handle* h, const void* src, void* tgt, int64_t
  * lbm_get_populations reads). */
 lbm_status lbm_population_buffer(lbm_handle* h, void** dev_ptr);
 
+/* ---- adjoint (no reference counterpart).  Differentiates a rollout of
+ * AB-push steps (prop_pattern AB, pull 0: the stored buffer is then the
+ * pre-collision state f^t) with respect to the per-cell force field and
+ * porosity.  All arrays below are device memory, FP64, planar with
+ * info.plane_stride elements per component.  The host drives checkpointed
+ * recomputation (lbmminiapp_gb300/adjoint.py). */
+enum { LBM_LOSS_NONE = 0, LBM_LOSS_VELOCITY = 1, LBM_LOSS_ENERGY = 2 };
+/* Copy the handle's current population buffer to (to_handle = 0) or from
+ * (to_handle = 1) a caller device buffer of info.buffer_bytes. */
+lbm_status lbm_copy_state(lbm_handle* h, void* dev, int to_handle);
+/* Per-cell force field [3][plane] and porosity [plane] from device memory;
+ * NULL removes the field. */
+lbm_status lbm_set_fields_device(lbm_handle* h, const double* force_field, const double* porosity);
+/* Loss of a state (NULL = the handle's current one):
+ *   LBM_LOSS_VELOCITY: time_weight * sum_x W(x).u(x), W [3][plane]
+ *   LBM_LOSS_ENERGY:   time_weight * sum_x W(x) rho |u|^2 / 2, W [plane]
+ * with u = (sum c f + F/2)/rho.  FP64; *out_host receives the value. */
+lbm_status lbm_loss(lbm_handle* h, const void* state, int loss_kind, const double* weight, double time_weight,
+                    double* out_host);
+/* One adjoint step: lam = dL/df^t from lam_next = dL/df^{t+1} and the state
+ * f^t (a buffer in the handle's storage); accumulates into grad_force
+ * [3][plane] and grad_porosity [plane] (either may be NULL).  collide = 0
+ * keeps only the loss term (the final state of a rollout); the loss term is
+ * added when loss_kind != LBM_LOSS_NONE. */
+lbm_status lbm_adjoint_step(lbm_handle* h, const void* state, const double* lam_next, double* lam, int collide,
+                            int loss_kind, const double* weight, double time_weight, double* grad_force,
+                            double* grad_porosity);
+
 /* ---- allocation-free conservation reduction.  No counterpart in the
  * reference.  For callers that cannot allocate device memory while they run
  * (hosts that give every device byte to their own pool at start-up, drivers

@@ -24,6 +24,7 @@ PATTERN_AB, PATTERN_AA = 0, 1
 STORE_F64, STORE_F32, STORE_BF16, STORE_F16 = 0, 1, 2, 3
 ARITH_AUTO, ARITH_F64, ARITH_F64X, ARITH_F32 = 0, 1, 2, 3
 LAYOUT_RAW, LAYOUT_LOGICAL = 0, 1
+LOSS_NONE, LOSS_VELOCITY, LOSS_ENERGY = 0, 1, 2
 
 STORAGE_NAMES = {"f64": STORE_F64, "f32": STORE_F32, "bf16": STORE_BF16, "f16": STORE_F16}
 ARITH_NAMES = {"auto": ARITH_AUTO, "f64": ARITH_F64, "f64x": ARITH_F64X, "f32": ARITH_F32}
@@ -74,6 +75,10 @@ _SIGNATURES = {
     "lbm_timestep_odd_force": (ctypes.c_int, [_P, _P, _I64, _I64]),
     "lbm_timestep_force": (ctypes.c_int, [_P, _P, _P, _I64, _I64]),
     "lbm_population_buffer": (ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    "lbm_copy_state": (ctypes.c_int, [_P, _P, ctypes.c_int]),
+    "lbm_set_fields_device": (ctypes.c_int, [_P, _P, _P]),
+    "lbm_loss": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_double, _P]),
+    "lbm_adjoint_step": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P, _P]),
     "lbm_reduce_conserved_noalloc": (ctypes.c_int, [ctypes.c_int] * 5 + [_I64, _P, _P, _P, ctypes.c_int, _P, _P]),
 }
 

@@ -29,6 +29,7 @@ SOURCES = [
     "lbm_step_q27_f64.cu",
     "lbm_step_q27_low.cu",
     "lbm_noalloc.cu",
+    "lbm_adjoint.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/lbm_gb300.h"
+#include "lbm_adjoint.cuh"
 #include "lbm_aux.cuh"
 #include "lbm_dispatch.cuh"
 #include "lbm_f64x.cuh"
@@ -727,6 +728,118 @@ lbm_status lbm_timestep_force(lbm_handle* h, const void* src, void* tgt, int64_t
    if (st != LBM_OK) return st;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
    return launch(h, h->cfg.pull ? K_AB_PULL : K_AB_PUSH, src, tgt, start, count);
+}
+
+lbm_status lbm_copy_state(lbm_handle* h, void* dev, int to_handle)
+{
+   if (!h || !dev) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   void* buf = const_cast<void*>(readout_buffer(h));
+   if (to_handle) LBM_CUDA(h, cudaMemcpyAsync(buf, dev, h->buffer_bytes, cudaMemcpyDeviceToDevice, h->stream));
+   else LBM_CUDA(h, cudaMemcpyAsync(dev, buf, h->buffer_bytes, cudaMemcpyDeviceToDevice, h->stream));
+   return LBM_OK;
+}
+
+namespace {
+__global__ void d2f_kernel(const double* src, float* dst, int64_t n)
+{
+   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+   if (i < n) dst[i] = (float)src[i];
+}
+}  // namespace
+
+static lbm_status set_field_device(lbm_handle* h, const double* dev, int ncomp, double** d64, float** d32)
+{
+   const size_t n = (size_t)h->plane * ncomp;
+   if (!dev) {
+      dev_free(h, *d64, sizeof(double) * n);
+      dev_free(h, *d32, sizeof(float) * n);
+      *d64 = nullptr;
+      *d32 = nullptr;
+      return LBM_OK;
+   }
+   if (h->storage == ST_F64) {
+      if (!*d64) {
+         lbm_status st = dev_alloc(h, (void**)d64, sizeof(double) * n);
+         if (st != LBM_OK) return st;
+      }
+      LBM_CUDA(h, cudaMemcpyAsync(*d64, dev, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+   } else {
+      if (!*d32) {
+         lbm_status st = dev_alloc(h, (void**)d32, sizeof(float) * n);
+         if (st != LBM_OK) return st;
+      }
+      d2f_kernel<<<blocks_for((int64_t)n, 256), 256, 0, h->stream>>>(dev, *d32, (int64_t)n);
+      LBM_CUDA(h, cudaGetLastError());
+      // the adjoint reads FP64 fields whatever the storage
+      if (!*d64) {
+         lbm_status st = dev_alloc(h, (void**)d64, sizeof(double) * n);
+         if (st != LBM_OK) return st;
+      }
+      LBM_CUDA(h, cudaMemcpyAsync(*d64, dev, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->stream));
+   }
+   return LBM_OK;
+}
+
+lbm_status lbm_set_fields_device(lbm_handle* h, const double* force_field, const double* porosity)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   lbm_status st = set_field_device(h, force_field, 3, &h->force_field, &h->force_field_f);
+   if (st == LBM_OK) st = set_field_device(h, porosity, 1, &h->porosity, &h->porosity_f);
+   return st;
+}
+
+static AdjParams adj_params(const lbm_handle* h, const void* state)
+{
+   AdjParams a;
+   std::memset(&a, 0, sizeof(a));
+   a.g = dims_of(h);
+   a.omega = h->cfg.omega;
+   for (int d = 0; d < 3; d++) a.F[d] = h->cfg.force[d];
+   a.links = h->links;
+   a.force_field = h->force_field;
+   a.porosity = h->porosity;
+   a.state = state ? state : readout_buffer(h);
+   return a;
+}
+
+lbm_status lbm_loss(lbm_handle* h, const void* state, int loss_kind, const double* weight, double time_weight,
+                    double* out_host)
+{
+   if (!h || !weight || !out_host || (loss_kind != LBM_LOSS_VELOCITY && loss_kind != LBM_LOSS_ENERGY))
+      return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   AdjParams a = adj_params(h, state);
+   a.loss_kind = loss_kind;
+   a.loss_weight = weight;
+   a.time_weight = time_weight;
+   LBM_CUDA(h, launch_loss(h->Q, h->storage, a, h->partials, kReduceBlocks, h->reduce_out, h->stream));
+   LBM_CUDA(h, cudaMemcpyAsync(out_host, h->reduce_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+   LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   return LBM_OK;
+}
+
+lbm_status lbm_adjoint_step(lbm_handle* h, const void* state, const double* lam_next, double* lam, int collide,
+                            int loss_kind, const double* weight, double time_weight, double* grad_force,
+                            double* grad_porosity)
+{
+   if (!h || !state || !lam || (collide && !lam_next)) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->cfg.prop_pattern != LBM_PATTERN_AB || h->cfg.pull)
+      return fail(h, LBM_ERR_STATE, "the adjoint differentiates AB-push rollouts");
+   if (loss_kind != LBM_LOSS_NONE && !weight) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   AdjParams a = adj_params(h, state);
+   a.lam_next = lam_next;
+   a.lam = lam;
+   a.collide = collide;
+   a.loss_kind = loss_kind;
+   a.loss_weight = weight;
+   a.time_weight = time_weight;
+   a.grad_force = grad_force;
+   a.grad_porosity = grad_porosity;
+   LBM_CUDA(h, launch_adjoint(h->Q, h->storage, a, h->stream));
+   return LBM_OK;
 }
 
 lbm_status lbm_population_buffer(lbm_handle* h, void** dev_ptr)
