@@ -123,8 +123,9 @@ class Rollout:
             self.seg = [self._alloc() for _ in range(self.K)]
         T = self.steps
         kind_T = self.kind if self._in_window(T) else N.LOSS_NONE
+        # seed: the final state's loss term (its direct force dependence included)
         self._check(self.lib.lbm_adjoint_step(self.h, _vp(self.final_state), None, _vp(lam_next), 0, kind_T,
-                                              _vp(self.weight), self.tw, None, None))
+                                              _vp(self.weight), self.tw, _vp(gF), _vp(gS)))
         nseg = len(self.ckpt)
         for k in reversed(range(nseg)):
             tb, te = k * self.K, min(T, (k + 1) * self.K)

@@ -96,7 +96,7 @@ def test_autograd_function_matches_run_backward(gpu):
     gF, gS = r.run_backward()
     assert torch.allclose(p.grad, r.from_plane(gS), rtol=1e-12, atol=0)
     assert torch.allclose(f.grad, r.from_plane(gF), rtol=1e-12, atol=0)
-    assert float(loss) > 0
+    assert float(loss.detach()) > 0
 
 
 @pytest.mark.parametrize("storage", ["f64", "f32"])
