@@ -58,7 +58,49 @@ def parse():
     ap.add_argument("--pattern", default="aa", choices=["aa", "ab_push", "ab_pull"])
     ap.add_argument("--accuracy", action="store_true",
                     help="print the mixed-precision error table (n^3, 1000 steps) instead of timing")
+    ap.add_argument("--porous", action="store_true",
+                    help="print the sphere-packing permeability / porosity-gradient study instead of timing")
+    ap.add_argument("--porous-n", type=int, default=384)
+    ap.add_argument("--porous-steps", type=int, default=2000)
     return ap.parse_args()
+
+
+def run_porous(args, device):
+    """D3Q27 AA sphere packing (radius 6-12, solid fraction 0.35, periodic),
+    g_x = 1e-6, tau = 0.7: permeability in FP64 / FP32 / BF16 / FP16 storage
+    and the mean-flux porosity gradient of the FP16 forward with the FP32
+    adjoint (checkpoints every 100 steps, sub-checkpoints every 10) against
+    the FP64-storage forward (F64X arithmetic, within 1e-10 of exact FP64)
+    with the FP64 adjoint (nested checkpoints of stride 3^6 .. 3, which fit
+    the FP64 states in device memory)."""
+    from lbmminiapp_gb300 import porous, workloads
+    n, steps, tau, gx = args.porous_n, args.porous_steps, 0.7, 1e-6
+    t0 = time.perf_counter()
+    solid, centres, radii = workloads.sphere_packing(n, 0.35, 6.0, 12.0, seed=2024)
+    t_pack = time.perf_counter() - t0
+    fluid = ~solid.astype(bool)
+    fw = {}
+    for st, ar in (("f64", "f64"), ("f64", "f64x"), ("f32", "auto"), ("bf16", "auto"), ("f16", "auto")):
+        fw[f"{st}/{ar}"] = porous.forward(solid, tau, gx, steps, storage=st, arithmetic=ar, device=device)
+    k64 = fw["f64/f64"]["permeability"]
+    for v in fw.values():
+        v["k_rel_err"] = abs(v["permeability"] - k64) / k64
+    L16, g16, t16 = porous.flux_gradient(solid, tau, gx, steps, (100, 10), storage="f16", adjoint="f32",
+                                         device=device)
+    L64, g64, t64 = porous.flux_gradient(solid, tau, gx, steps, (729, 243, 81, 27, 9, 3), storage="f64",
+                                         adjoint="f64", arithmetic="f64x", device=device)
+    out = {"porous": "D3Q27 AA periodic sphere packing", "grid": [n] * 3, "spheres": int(len(radii)),
+           "solid_fraction": float(solid.mean()), "radius": [6, 12], "seed": 2024, "tau": tau, "gx": gx,
+           "steps": steps, "packing_seconds": round(t_pack, 1),
+           "forward": {k: {kk: (round(vv, 3) if kk in ("seconds", "mflups") else vv) for kk, vv in v.items()}
+                       for k, v in fw.items()},
+           "gradient": {"loss_f16_f32adj": L16, "loss_f64": L64, "loss_rel_err": abs(L16 - L64) / abs(L64),
+                        "seconds_f16_f32adj": round(t16, 1), "seconds_f64": round(t64, 1),
+                        "checkpoints_f16": [100, 10], "checkpoints_f64": [729, 243, 81, 27, 9, 3],
+                        "reference": "FP64 storage, F64X forward, FP64 adjoint",
+                        **porous.gradient_errors(g16, g64, fluid)}}
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def dist_setup(args):
@@ -224,6 +266,8 @@ def main():
         return 0
 
     torch.cuda.set_device(local)
+    if args.porous:
+        return run_porous(args, local)
     n = args.n
     ncell = n ** 3
     Q = args.lattice
@@ -265,7 +309,10 @@ def main():
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic_per_launch() if headline else None,
                 "peak_kind": f"{peak_kind} copy bandwidth",
-                "kernel": f"step_kernel<{Q},{args.storage},{arith},{args.pattern}> (one launch per step)",
+                "kernel": (f"step_async_kernel<{Q},{args.pattern}> (F64X, persistent warps, cp.async-prefetched "
+                           f"tiles of 32 cells; one launch per step)"
+                           if arith == "f64x" and n % 32 == 0 else
+                           f"step_kernel<{Q},{args.storage},{arith},{args.pattern}> (one launch per step)"),
                 "algorithmic_bytes_per_launch": ncell * bpu}
 
     # end to end through the C ABI, pinned host buffers

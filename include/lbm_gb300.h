@@ -200,6 +200,12 @@ lbm_status lbm_loss(lbm_handle* h, const void* state, int loss_kind, const doubl
 lbm_status lbm_adjoint_step(lbm_handle* h, const void* state, const double* lam_next, double* lam, int collide,
                             int loss_kind, const double* weight, double time_weight, double* grad_force,
                             double* grad_porosity);
+/* lbm_adjoint_step with lam, lam_next and the arithmetic in FP32 (on the
+ * deviations f - w); grad_force and grad_porosity are still FP64 accumulators.
+ * For rollouts whose forward runs in reduced-precision storage. */
+lbm_status lbm_adjoint_step_f32(lbm_handle* h, const void* state, const float* lam_next, float* lam, int collide,
+                                int loss_kind, const double* weight, double time_weight, double* grad_force,
+                                double* grad_porosity);
 
 /* ---- allocation-free conservation reduction.  No counterpart in the
  * reference.  For callers that cannot allocate device memory while they run

@@ -79,6 +79,7 @@ _SIGNATURES = {
     "lbm_set_fields_device": (ctypes.c_int, [_P, _P, _P]),
     "lbm_loss": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_double, _P]),
     "lbm_adjoint_step": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P, _P]),
+    "lbm_adjoint_step_f32": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P, _P]),
     "lbm_reduce_conserved_noalloc": (ctypes.c_int, [ctypes.c_int] * 5 + [_I64, _P, _P, _P, ctypes.c_int, _P, _P]),
 }
 

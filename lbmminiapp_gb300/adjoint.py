@@ -9,11 +9,20 @@ state and accumulates a loss over a window of steps
 
 with u = (sum c f + F/2) / rho.  The gradient with respect to the per-cell
 force field F(x) and porosity (partial bounce-back solid fraction) s(x) comes
-from the hand-written adjoint kernel (``lbm_adjoint_step``).  The forward
-stores the state every ``checkpoint_every`` steps; the reverse sweep recomputes
-each segment from its checkpoint into ``checkpoint_every`` state buffers and
-runs the adjoint back through it.  Device memory: (steps / checkpoint_every +
-checkpoint_every + 1) population buffers plus three FP64 adjoint buffers.
+from the hand-written adjoint kernel: ``lbm_adjoint_step`` (FP64) or
+``lbm_adjoint_step_f32`` (adjoint state and arithmetic in FP32, gradients
+accumulated in FP64), chosen by ``adjoint="f64" | "f32"``.
+
+Checkpointing is multi-level.  ``checkpoint_every`` is one stride S_0 or a
+decreasing tuple (S_0, S_1, ..., S_{L-1}).  The forward stores the state at
+every multiple of S_0.  The reverse sweep takes the level-0 segments last to
+first; a segment of level l < L is recomputed from its checkpoint, storing the
+state at every S_{l+1}-th step (level l+1 checkpoints), and its sub-segments
+are reversed the same way; a segment of level L (at most S_{L-1} steps) is
+recomputed storing every state and the adjoint runs back through it.  State
+buffers held at once: ceil(steps / S_0) + sum_l (ceil(S_{l-1} / S_l) - 1) +
+S_{L-1} - 1 + 1 (the final state), plus two adjoint buffers; each level of
+checkpoints costs one more forward pass in recomputation.
 
 Device arrays (torch, float64, CUDA) are planar with ``plane`` elements per
 component; :meth:`Rollout.to_plane` / :meth:`Rollout.from_plane` convert from
@@ -22,6 +31,7 @@ and to (nz, ny, nx) arrays.
 from __future__ import annotations
 
 import ctypes
+import math
 
 import numpy as np
 import torch
@@ -36,16 +46,33 @@ def _vp(t):
     return None if t is None else ctypes.c_void_p(t.data_ptr())
 
 
+def checkpoint_buffers(steps, strides):
+    """State buffers a rollout of ``steps`` with these checkpoint strides holds
+    at once (the final state's included, the handle's own not)."""
+    strides = (strides,) if isinstance(strides, int) else tuple(strides)
+    n = math.ceil(steps / strides[0]) + max(1, strides[-1] - 1)
+    for a, b in zip(strides[:-1], strides[1:]):
+        n += math.ceil(a / b) - 1
+    return n
+
+
 class Rollout:
-    def __init__(self, sim: Simulation, steps: int, checkpoint_every: int, loss: str, weight, window,
-                 time_weight: float = 1.0):
+    def __init__(self, sim: Simulation, steps: int, checkpoint_every, loss: str, weight, window,
+                 time_weight: float = 1.0, adjoint: str = "f64", device=None):
         if sim.pattern != "ab_push":
             raise ValueError("the adjoint differentiates AB-push rollouts (pattern='ab_push')")
+        if adjoint not in ("f64", "f32"):
+            raise ValueError("adjoint must be 'f64' or 'f32'")
+        strides = (checkpoint_every,) if isinstance(checkpoint_every, int) else tuple(checkpoint_every)
+        if not strides or any(int(a) <= int(b) for a, b in zip(strides[:-1], strides[1:])) or int(strides[-1]) < 1:
+            raise ValueError("checkpoint strides must be positive and strictly decreasing")
         self.sim = sim
         self.lib = sim.lib
         self.h = sim.h
         self.steps = int(steps)
-        self.K = int(checkpoint_every)
+        self.strides = tuple(int(v) for v in strides)
+        self.K = self.strides[0]
+        self.adjoint = adjoint
         self.kind = LOSS_KINDS[loss]
         self.t0, self.t1 = int(window[0]), int(window[1])
         self.tw = float(time_weight)
@@ -54,7 +81,7 @@ class Rollout:
         self.plane = int(info.plane_stride)
         self.ncell = sim.ncell
         self.buffer_bytes = int(info.buffer_bytes)
-        self.dev = torch.device("cuda", sim.cfg.device)
+        self.dev = torch.device("cuda", sim.cfg.device) if device is None else torch.device(device)
         w = torch.as_tensor(weight, dtype=torch.float64)
         if loss == "velocity":
             self.weight = self.to_plane(w.reshape(3, -1), ncomp=3)
@@ -62,15 +89,25 @@ class Rollout:
             self.weight = self.to_plane(w.reshape(1, -1), ncomp=1)
         self.force_field = None
         self.porosity = None
-        self._alloc = lambda: torch.empty(self.buffer_bytes, dtype=torch.uint8, device=self.dev)
+        # the initial state is the first level-0 checkpoint
         self.init_state = self._alloc()
         self._check(self.lib.lbm_copy_state(self.h, _vp(self.init_state), 0))
         nseg = (self.steps + self.K - 1) // self.K
-        self.ckpt = [self._alloc() for _ in range(nseg)]
+        self.ckpt = [self.init_state] + [self._alloc() for _ in range(nseg - 1)]
         self.final_state = self._alloc()
-        self.seg = None
+        self._pools = {}
 
     # ------------------------------------------------------------ helpers
+    def _alloc(self):
+        return torch.empty(self.buffer_bytes, dtype=torch.uint8, device=self.dev)
+
+    def release(self):
+        """Drop every state buffer (checkpoints, recomputation pools, the
+        initial and final states); the rollout cannot run afterwards."""
+        self.ckpt = []
+        self._pools = {}
+        self.init_state = self.final_state = None
+
     def _check(self, st):
         N.check(st, self.h)
 
@@ -94,52 +131,91 @@ class Rollout:
     def _in_window(self, t):
         return self.t0 <= t <= self.t1
 
+    def _pool(self, level, n):
+        pool = self._pools.setdefault(level, [])
+        while len(pool) < n:
+            pool.append(self._alloc())
+        return pool[:n]
+
+    def _save(self, buf):
+        self._check(self.lib.lbm_copy_state(self.h, _vp(buf), 0))
+
+    def _load(self, buf):
+        self._check(self.lib.lbm_copy_state(self.h, _vp(buf), 1))
+
     # ------------------------------------------------------------ forward
     def run_forward(self, store=True) -> float:
-        self._check(self.lib.lbm_copy_state(self.h, _vp(self.init_state), 1))
+        self._load(self.init_state)
         loss = 0.0
         out = ctypes.c_double(0.0)
         for t in range(self.steps):
-            if store and t % self.K == 0:
-                self._check(self.lib.lbm_copy_state(self.h, _vp(self.ckpt[t // self.K]), 0))
+            if store and t % self.K == 0 and t > 0:
+                self._save(self.ckpt[t // self.K])
             self.sim.step(1)
             if self._in_window(t + 1):
                 self._check(self.lib.lbm_loss(self.h, None, self.kind, _vp(self.weight), self.tw, ctypes.byref(out)))
                 loss += out.value
         if store:
-            self._check(self.lib.lbm_copy_state(self.h, _vp(self.final_state), 0))
+            self._save(self.final_state)
         self.sim.synchronize()
         return loss
 
     # ------------------------------------------------------------ adjoint
-    def run_backward(self):
-        """(grad_force (3, plane), grad_porosity (plane,)) after run_forward(store=True)."""
-        Q, P = self.Q, self.plane
-        lam_next = torch.zeros((Q, P), dtype=torch.float64, device=self.dev)
-        lam = torch.zeros_like(lam_next)
-        gF = torch.zeros((3, P), dtype=torch.float64, device=self.dev)
-        gS = torch.zeros((P,), dtype=torch.float64, device=self.dev)
-        if self.seg is None:
-            self.seg = [self._alloc() for _ in range(self.K)]
-        T = self.steps
-        kind_T = self.kind if self._in_window(T) else N.LOSS_NONE
-        # seed: the final state's loss term (its direct force dependence included)
-        self._check(self.lib.lbm_adjoint_step(self.h, _vp(self.final_state), None, _vp(lam_next), 0, kind_T,
-                                              _vp(self.weight), self.tw, _vp(gF), _vp(gS)))
-        nseg = len(self.ckpt)
-        for k in reversed(range(nseg)):
-            tb, te = k * self.K, min(T, (k + 1) * self.K)
-            self._check(self.lib.lbm_copy_state(self.h, _vp(self.ckpt[k]), 1))
-            for i in range(te - tb):
-                self._check(self.lib.lbm_copy_state(self.h, _vp(self.seg[i]), 0))
-                if i < te - tb - 1:
+    def _adjoint_step(self, state, t, collide):
+        """lam <- dL/df^t from lam_next = dL/df^{t+1}, then swap the two."""
+        kind = self.kind if self._in_window(t) else N.LOSS_NONE
+        fn = self.lib.lbm_adjoint_step_f32 if self.adjoint == "f32" else self.lib.lbm_adjoint_step
+        self._check(fn(self.h, _vp(state), _vp(self._lam_next) if collide else None,
+                       _vp(self._lam if collide else self._lam_next), collide, kind, _vp(self.weight), self.tw,
+                       _vp(self._gF), _vp(self._gS)))
+        if collide:
+            self._lam, self._lam_next = self._lam_next, self._lam
+
+    def _reverse(self, a, b, level, buf):
+        """Adjoint from lam^b (in lam_next) to lam^a over the steps [a, b),
+        with f^a in buf."""
+        if level == len(self.strides):
+            states = [buf] + self._pool(level, b - a - 1)
+            if b - a > 1:
+                self._load(buf)
+                for i in range(1, b - a):
                     self.sim.step(1)
-            for t in range(te - 1, tb - 1, -1):
-                kind = self.kind if self._in_window(t) else N.LOSS_NONE
-                self._check(self.lib.lbm_adjoint_step(self.h, _vp(self.seg[t - tb]), _vp(lam_next), _vp(lam), 1,
-                                                      kind, _vp(self.weight), self.tw, _vp(gF), _vp(gS)))
-                lam, lam_next = lam_next, lam
+                    self._save(states[i])
+            for t in range(b - 1, a - 1, -1):
+                self._adjoint_step(states[t - a], t, 1)
+            return
+        S = self.strides[level]
+        starts = list(range(a, b, S))
+        subs = [buf] + self._pool(level, len(starts) - 1)
+        if len(starts) > 1:
+            self._load(buf)
+            for i in range(1, len(starts)):
+                self.sim.step(S)
+                self._save(subs[i])
+        for i in reversed(range(len(starts))):
+            self._reverse(starts[i], min(b, starts[i] + S), level + 1, subs[i])
+
+    def run_backward(self, grad_force=True):
+        """(grad_force (3, plane) or None, grad_porosity (plane,)) after
+        run_forward(store=True)."""
+        Q, P = self.Q, self.plane
+        ldt = torch.float32 if self.adjoint == "f32" else torch.float64
+        self._lam_next = torch.zeros((Q, P), dtype=ldt, device=self.dev)
+        self._lam = torch.zeros_like(self._lam_next)
+        self._gF = torch.zeros((3, P), dtype=torch.float64, device=self.dev) if grad_force else None
+        self._gS = torch.zeros((P,), dtype=torch.float64, device=self.dev)
+        T = self.steps
+        # seed: the final state's loss term (its direct force dependence
+        # included); its buffer then serves the finest level's recomputation
+        self._adjoint_step(self.final_state, T, 0)
+        finest = self._pools.setdefault(len(self.strides), [])
+        if not any(b is self.final_state for b in finest):
+            finest.insert(0, self.final_state)
+        for k in reversed(range(len(self.ckpt))):
+            self._reverse(k * self.K, min(T, (k + 1) * self.K), 1, self.ckpt[k])
         self.sim.synchronize()
+        gF, gS = self._gF, self._gS
+        self._lam = self._lam_next = self._gF = self._gS = None
         return gF, gS
 
 
@@ -176,9 +252,11 @@ def outlet_weight(shape, solid, x_plane, window_len):
 
 
 def new_rollout(nx, ny, nz, lattice, tau, solid, periodic, steps, checkpoint_every, loss, weight, window,
-                storage="f64", force=(0.0, 0.0, 0.0), u0=None, device=0):
+                storage="f64", force=(0.0, 0.0, 0.0), u0=None, device=0, adjoint="f64", arithmetic=None):
+    if arithmetic is None:
+        arithmetic = "f64" if storage == "f64" else "auto"
     sim = Simulation(nx, ny, nz, lattice=lattice, pattern="ab_push", omega=1.0 / tau, force=force, periodic=periodic,
-                     storage=storage, arithmetic="f64" if storage == "f64" else "auto", device=device)
+                     storage=storage, arithmetic=arithmetic, device=device)
     sim.set_solid(solid)
     sim.init_equilibrium(None, u0)
-    return Rollout(sim, steps, checkpoint_every, loss, weight, window)
+    return Rollout(sim, steps, checkpoint_every, loss, weight, window, adjoint=adjoint)

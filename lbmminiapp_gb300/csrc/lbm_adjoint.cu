@@ -26,7 +26,12 @@
 // Loss terms at step t (weight tw, spatial weights W):
 //   velocity:  L_t = tw sum_x W(x) . u(x)        dL/df_k = tw W.(c_k - u)/rho, dL/dF = tw W/(2 rho)
 //   energy:    L_t = tw sum_x W_0(x) rho|u|^2/2   dL/df_k = tw W_0 (u.c_k - |u|^2/2), dL/dF = tw W_0 u/2
-// All in FP64; f^t may be stored in any storage format.
+// adjoint_step_kernel works in FP64.  adjoint_step_f32_kernel is the same
+// step with lam and the arithmetic in FP32, written on the deviations
+// g_s = f_s - w_s (the shifted storage formats hold exactly these), so that
+// f_opp(s) - C_s = g_opp(s) - (C_s - w_s) has no cancellation against w; its
+// gradients are still accumulated in FP64.  f^t may be stored in any storage
+// format.
 #include <cuda_runtime.h>
 
 #include "../../include/lbm_gb300.h"
@@ -167,6 +172,146 @@ __global__ void __launch_bounds__(128) adjoint_step_kernel(AdjParams a)
    if (a.grad_porosity) a.grad_porosity[c] += gsig;
 }
 
+// FP32 deviation g = f - w of a stored population.
+template <int ST>
+__device__ __forceinline__ float load_dev(const void* buf, int64_t idx, double w)
+{
+   if constexpr (ST == ST_F64) {
+      return (float)(static_cast<const double*>(buf)[idx] - w);
+   } else {
+      return load_shifted(static_cast<const typename Store<ST>::T*>(buf) + idx);
+   }
+}
+
+template <int Q, int ST>
+__global__ void __launch_bounds__(256) adjoint_step_f32_kernel(AdjParams a)
+{
+   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+   int x, y, z;
+   if (!cell_xyz(a.g, c, x, y, z)) return;
+   const uint32_t lk = a.links ? a.links[c] : 0u;
+   if (lk & kSolidBit) {
+#pragma unroll
+      for (int s = 0; s < Q; s++) a.lam_f[(int64_t)s * a.g.plane + c] = 0.0f;
+      return;
+   }
+   float g[Q];
+#pragma unroll
+   for (int s = 0; s < Q; s++) g[s] = load_dev<ST>(a.state, (int64_t)s * a.g.plane + c, lat_w(Q, s));
+   float F[3] = {(float)a.F[0], (float)a.F[1], (float)a.F[2]};
+   if (a.force_field) {
+      F[0] = (float)(a.F[0] + a.force_field[c]);
+      F[1] = (float)(a.F[1] + a.force_field[a.g.plane + c]);
+      F[2] = (float)(a.F[2] + a.force_field[2 * a.g.plane + c]);
+   }
+   const float sig = a.porosity ? (float)a.porosity[c] : 0.0f;
+   float drho = 0.0f, j[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      drho += g[s];
+      j[0] += g[s] * (float)lat_c(Q, s, 0);
+      j[1] += g[s] * (float)lat_c(Q, s, 1);
+      j[2] += g[s] * (float)lat_c(Q, s, 2);
+   }
+   const float rho = 1.0f + drho;
+   const float ir = 1.0f / rho;
+   float u[3];
+#pragma unroll
+   for (int d = 0; d < 3; d++) {
+      j[d] += 0.5f * F[d];
+      u[d] = j[d] * ir;
+   }
+   const float uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+   const float Fu = F[0] * u[0] + F[1] * u[1] + F[2] * u[2];
+   const float om = (float)a.omega, om1 = (float)(1.0 - a.omega), om2 = (float)(1.0 - 0.5 * a.omega);
+
+   float lam[Q];
+#pragma unroll
+   for (int s = 0; s < Q; s++) lam[s] = 0.0f;
+   float gF[3] = {0.0f, 0.0f, 0.0f};
+   float gsig = 0.0f;
+
+   if (a.collide) {
+      float mu[Q];
+#pragma unroll
+      for (int s = 0; s < Q; s++) {
+         if (s == lat_rest(Q)) {
+            mu[s] = a.lam_next_f[(int64_t)s * a.g.plane + c];
+         } else if ((lk >> s) & 1u) {
+            mu[s] = a.lam_next_f[(int64_t)lat_opp(Q, s) * a.g.plane + c];
+         } else {
+            const int64_t n = nbr_cell(a.g, x, y, z, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+            mu[s] = a.lam_next_f[(int64_t)s * a.g.plane + n];
+         }
+      }
+      float Arho = 0.0f, Aj[3] = {0.0f, 0.0f, 0.0f}, GF[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int s = 0; s < Q; s++) {
+         const float c0 = (float)lat_c(Q, s, 0), c1 = (float)lat_c(Q, s, 1), c2 = (float)lat_c(Q, s, 2);
+         const float w = (float)lat_w(Q, s);
+         const float cu = c0 * u[0] + c1 * u[1] + c2 * u[2];
+         const float cF = c0 * F[0] + c1 * F[1] + c2 * F[2];
+         const float cj = c0 * j[0] + c1 * j[1] + c2 * j[2];
+         // C_s - w_s for the porosity gradient
+         const float eqd = w * (drho + 3.0f * cj + 4.5f * cj * cu - 1.5f * uu * rho);
+         const float fd = w * (3.0f * cF - 3.0f * Fu + 9.0f * cu * cF);
+         const float Cd = om1 * g[s] + om * eqd + om2 * fd;
+         gsig += mu[s] * (g[lat_opp(Q, s)] - Cd);
+         const float nu = (1.0f - sig) * mu[s];
+         lam[s] += om1 * nu;
+         lam[lat_opp(Q, s)] += sig * mu[s];
+         const float deq_drho = w * (1.0f - 4.5f * cu * cu + 1.5f * uu);
+         const float dfd_drho = w * (3.0f * Fu - 9.0f * cu * cF) * ir;
+         Arho += nu * (om * deq_drho + om2 * dfd_drho);
+         const float kc = nu * w * (om * (3.0f + 9.0f * cu) + om2 * 9.0f * cF * ir);
+         Aj[0] += kc * c0 - nu * w * (om * 3.0f * u[0] + om2 * 3.0f * F[0] * ir);
+         Aj[1] += kc * c1 - nu * w * (om * 3.0f * u[1] + om2 * 3.0f * F[1] * ir);
+         Aj[2] += kc * c2 - nu * w * (om * 3.0f * u[2] + om2 * 3.0f * F[2] * ir);
+         const float kf = nu * om2 * w;
+         GF[0] += kf * (3.0f * c0 - 3.0f * u[0] + 9.0f * cu * c0);
+         GF[1] += kf * (3.0f * c1 - 3.0f * u[1] + 9.0f * cu * c1);
+         GF[2] += kf * (3.0f * c2 - 3.0f * u[2] + 9.0f * cu * c2);
+      }
+#pragma unroll
+      for (int s = 0; s < Q; s++)
+         lam[s] += Arho + Aj[0] * (float)lat_c(Q, s, 0) + Aj[1] * (float)lat_c(Q, s, 1) +
+                   Aj[2] * (float)lat_c(Q, s, 2);
+#pragma unroll
+      for (int d = 0; d < 3; d++) gF[d] = GF[d] + 0.5f * Aj[d];
+   }
+
+   if (a.loss_kind == LBM_LOSS_VELOCITY && a.loss_weight) {
+      const float tw = (float)a.time_weight;
+      const float W[3] = {(float)a.loss_weight[c], (float)a.loss_weight[a.g.plane + c],
+                          (float)a.loss_weight[2 * a.g.plane + c]};
+      const float Wu = W[0] * u[0] + W[1] * u[1] + W[2] * u[2];
+#pragma unroll
+      for (int s = 0; s < Q; s++) {
+         const float Wc = W[0] * (float)lat_c(Q, s, 0) + W[1] * (float)lat_c(Q, s, 1) + W[2] * (float)lat_c(Q, s, 2);
+         lam[s] += tw * (Wc - Wu) * ir;
+      }
+#pragma unroll
+      for (int d = 0; d < 3; d++) gF[d] += tw * W[d] * 0.5f * ir;
+   } else if (a.loss_kind == LBM_LOSS_ENERGY && a.loss_weight) {
+      const float tw = (float)(a.time_weight * a.loss_weight[c]);
+#pragma unroll
+      for (int s = 0; s < Q; s++) {
+         const float uc = u[0] * (float)lat_c(Q, s, 0) + u[1] * (float)lat_c(Q, s, 1) + u[2] * (float)lat_c(Q, s, 2);
+         lam[s] += tw * (uc - 0.5f * uu);
+      }
+#pragma unroll
+      for (int d = 0; d < 3; d++) gF[d] += tw * 0.5f * u[d];
+   }
+
+#pragma unroll
+   for (int s = 0; s < Q; s++) a.lam_f[(int64_t)s * a.g.plane + c] = lam[s];
+   if (a.grad_force) {
+#pragma unroll
+      for (int d = 0; d < 3; d++) a.grad_force[(int64_t)d * a.g.plane + c] += (double)gF[d];
+   }
+   if (a.grad_porosity) a.grad_porosity[c] += (double)gsig;
+}
+
 // Loss value of the current state (FP64 partial sums per block).
 template <int Q, int ST>
 __global__ void __launch_bounds__(kReduceThreads) loss_partial_kernel(AdjParams a, double* partials)
@@ -233,6 +378,13 @@ cudaError_t launch_adjoint_t(const AdjParams& a, cudaStream_t st)
 }
 
 template <int Q, int ST>
+cudaError_t launch_adjoint_f32_t(const AdjParams& a, cudaStream_t st)
+{
+   adjoint_step_f32_kernel<Q, ST><<<(unsigned)((a.g.ncell + 255) / 256), 256, 0, st>>>(a);
+   return cudaGetLastError();
+}
+
+template <int Q, int ST>
 cudaError_t launch_loss_t(const AdjParams& a, double* partials, int nblocks, double* out, cudaStream_t st)
 {
    loss_partial_kernel<Q, ST><<<nblocks, kReduceThreads, 0, st>>>(a, partials);
@@ -255,6 +407,11 @@ cudaError_t launch_loss_t(const AdjParams& a, double* partials, int nblocks, dou
 cudaError_t launch_adjoint(int Q, int st, const AdjParams& a, cudaStream_t stream)
 {
    LBM_ADJ_DISPATCH(launch_adjoint_t, a, stream)
+}
+
+cudaError_t launch_adjoint_f32(int Q, int st, const AdjParams& a, cudaStream_t stream)
+{
+   LBM_ADJ_DISPATCH(launch_adjoint_f32_t, a, stream)
 }
 
 cudaError_t launch_loss(int Q, int st, const AdjParams& a, double* partials, int nblocks, double* out,

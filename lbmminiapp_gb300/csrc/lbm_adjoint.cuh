@@ -23,9 +23,12 @@ struct AdjParams {
    double time_weight;
    int loss_kind;
    int collide;                   // 0: loss term only (the last state of a rollout)
+   const float* lam_next_f;       // FP32 adjoint: [Q][plane]
+   float* lam_f;                  // FP32 adjoint: [Q][plane]
 };
 
 cudaError_t launch_adjoint(int Q, int storage, const AdjParams& a, cudaStream_t stream);
+cudaError_t launch_adjoint_f32(int Q, int storage, const AdjParams& a, cudaStream_t stream);
 cudaError_t launch_loss(int Q, int storage, const AdjParams& a, double* partials, int nblocks, double* out,
                         cudaStream_t stream);
 

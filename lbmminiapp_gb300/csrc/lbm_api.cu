@@ -181,6 +181,9 @@ KParams make_params(const lbm_handle* h, int64_t start, int64_t end, Launch& L)
    const int pbx = (int)std::min<int64_t>(256, ((half + 31) / 32) * 32);
    L.pair_block = dim3(pbx, 1, 1);
    L.pair_grid = dim3((half + pbx - 1) / pbx, c.ny, (unsigned)(z1 - z0));
+   L.async = h->storage == ST_F64 && h->arith == AR_F64X && c.nx % 32 == 0 && start == 0 && end == h->ncell &&
+             L.idx32;
+   L.ag = async_geom(c.nx, c.ny, c.nz);
    return p;
 }
 
@@ -839,6 +842,28 @@ lbm_status lbm_adjoint_step(lbm_handle* h, const void* state, const double* lam_
    a.grad_force = grad_force;
    a.grad_porosity = grad_porosity;
    LBM_CUDA(h, launch_adjoint(h->Q, h->storage, a, h->stream));
+   return LBM_OK;
+}
+
+lbm_status lbm_adjoint_step_f32(lbm_handle* h, const void* state, const float* lam_next, float* lam, int collide,
+                                int loss_kind, const double* weight, double time_weight, double* grad_force,
+                                double* grad_porosity)
+{
+   if (!h || !state || !lam || (collide && !lam_next)) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->cfg.prop_pattern != LBM_PATTERN_AB || h->cfg.pull)
+      return fail(h, LBM_ERR_STATE, "the adjoint differentiates AB-push rollouts");
+   if (loss_kind != LBM_LOSS_NONE && !weight) return LBM_ERR_INVALID_ARGUMENT;
+   LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   AdjParams a = adj_params(h, state);
+   a.lam_next_f = lam_next;
+   a.lam_f = lam;
+   a.collide = collide;
+   a.loss_kind = loss_kind;
+   a.loss_weight = weight;
+   a.time_weight = time_weight;
+   a.grad_force = grad_force;
+   a.grad_porosity = grad_porosity;
+   LBM_CUDA(h, launch_adjoint_f32(h->Q, h->storage, a, h->stream));
    return LBM_OK;
 }
 

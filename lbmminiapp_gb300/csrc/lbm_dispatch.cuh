@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "lbm_step.cuh"
+#include "lbm_step_async.cuh"
 
 namespace lbm {
 
@@ -15,6 +16,8 @@ struct Launch {
    bool idx32;   // plane stride below 2^32 bytes: 32-bit stride arithmetic
    bool pair;    // two cells per thread (shifted storage, periodic box, even nx, full grid)
    dim3 pair_grid, pair_block;
+   bool async;   // pipelined persistent kernel (FP64 storage, F64X, nx % 32 == 0, full grid)
+   AsyncGeom ag;
 };
 
 template <int Q, int ST, int AR, int KIND>
@@ -30,6 +33,9 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
          else step_pair_kernel<Q, ST, KIND, int64_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
          return cudaGetLastError();
       }
+   }
+   if constexpr (ST == ST_F64 && AR == AR_F64X) {
+      if (L.async && !links && !fields) return launch_async<Q, KIND>(p, L.ag, src, dst, L.stream);
    }
    // Per-cell fields always use the exact FP64 arithmetic when FP64 is stored.
    constexpr int ARF = (AR == AR_F64X) ? AR_F64 : AR;

@@ -1,23 +1,26 @@
 // F64X: double-precision BGK collision computed without the FP64 pipe.
 //
 // GB300's FP64 units run at about 1/60 of its FP32 rate, and double <-> float
-// conversions go through them too, so a collision written in `double` is
-// compute-bound far below the HBM roofline.  This path keeps the populations
+// conversions are slow as well, so a collision written in `double` (or in
+// float with conversions at load and store) is compute-bound far below the
+// HBM roofline.  This path keeps the populations
 // in FP64 memory (the reference's Pdf buffers) but:
 //
 //  * splits each loaded double into an unevaluated float pair (h, l) with
 //    integer operations only: h is the double truncated to 24 significant
-//    bits, l the next 23 bits (|f - (h + l)| < 2^-47 |f|);
+//    bits, l the remaining bits rounded to 23 (|f - (h + l)| <= 2^-48 |f|);
 //  * evaluates rho, j = sum c f, u, the equilibrium and the BGK/Guo update in
 //    double-float arithmetic built from the error-free transformations
 //    TwoSum (Knuth), Fast2Sum (Dekker 1971) and the FMA two-product, as used
 //    in double-double libraries (Hida, Li & Bailey, "Library for double-double
 //    and quad-double arithmetic", 2001);
-//  * rebuilds the 64-bit pattern of the result with integer operations.
+//  * rebuilds the 64-bit pattern of the result (the double nearest to h + l)
+//    with integer operations and one float-to-int conversion.
 //
-// The fast path covers positive populations in [2^-80, 1), the only values a
-// physical state holds.  A cell whose inputs or results fall outside that
-// range is recomputed with the exact IEEE double collision, so any state is
+// The fast path covers positive populations in [2^-75, 1), the only values a
+// physical state holds (with further bounds on the rest population and the
+// velocity, checked per cell).  A cell whose inputs or results fall outside
+// them is recomputed with the exact IEEE double collision, so any state is
 // handled; the fast path's results agree with the exact path to about
 // 2^-46 relative per step.
 #pragma once
@@ -228,23 +231,6 @@ __host__ __device__ __forceinline__ df split(uint64_t bits)
    return {bitsf(hb), fsub(bitsf(xb), bitsf(mb))};
 }
 
-// Rebuild the double pattern of h + l (positive, result in [2^-80, 1)):
-//   S   = h + l rounded toward zero (so the remainder E >= 0 stays inside
-//         S's binade), E = the remainder;
-//   the pattern of S as a double, plus E counted in units of 2^7 double
-//   ulps of S, rounded with the 1.5*2^23 magic constant.
-__host__ __device__ __forceinline__ uint64_t join(df v)
-{
-   const float S = fadd_rz(v.h, v.l);
-   const float E = fsub(v.l, fsub(S, v.h));
-   const uint32_t sb = fbits(S);
-   const float scale = bitsf(0x95800000u - (sb & 0x7F800000u));  // 2^(45 - e(S))
-   const float y = ffma(E, scale, 12582912.0f);
-   const int32_t ei = (int32_t)(fbits(y) - 0x4B400000u);
-   const uint64_t d0 = ((uint64_t)sb << 29) + ((uint64_t)0x38000000u << 32);
-   return d0 + (uint64_t)((int64_t)ei * 128);
-}
-
 __host__ __device__ __forceinline__ int32_t f2i_rn(float x)
 {
 #ifdef __CUDA_ARCH__
@@ -271,19 +257,6 @@ __host__ __device__ __forceinline__ uint64_t join_checked(df v, bool& ok)
    const int32_t n = f2i_rn(fmul(E, scale));
    const uint64_t d0 = ((uint64_t)sb << 29) + ((uint64_t)0x38000000u << 32);
    return d0 + (uint64_t)(int64_t)n;
-}
-
-__host__ __device__ __forceinline__ bool in_range(uint64_t bits)
-{
-   const uint32_t hi = (uint32_t)(bits >> 32);
-   return hi >= kHiMin && hi < kHiMax;
-}
-
-// Result check before join: positive and inside the fast range.
-__host__ __device__ __forceinline__ bool out_ok(df v)
-{
-   const float s = fadd(v.h, v.l);
-   return s >= 8.271806125530277e-25f /* 2^-80 */ && s < 0.99999994f;
 }
 
 __host__ __device__ __forceinline__ double as_double(uint64_t b)

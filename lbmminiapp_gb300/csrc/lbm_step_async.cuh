@@ -1,0 +1,161 @@
+// Software-pipelined step kernel for FP64 storage with F64X arithmetic in a
+// fully periodic box (no link words, no per-cell fields).
+//
+// The F64X collision is about 1.7k instructions per cell, so the plain
+// one-cell-per-thread kernel spends its time either issuing or waiting on its
+// 19/27 loads with only 16 warps per SM resident (128 registers per thread).
+// Here every warp is persistent and works on tiles of 32 consecutive cells of
+// one x row: while it collides tile k it already has the loads of tile k+1 in
+// flight as cp.async copies (8 bytes per thread and direction) into its own
+// two-stage shared-memory buffer, so the loads hold no registers and their
+// latency overlaps the collision.  Each thread reads back only what it copied
+// itself, so cp.async.wait_group is the only synchronisation needed.
+//
+// AA (in place) stays race-free under the prefetch: the locations a cell's
+// thread reads are exactly the ones it writes (even step: its own slots; odd
+// step: slot s at x - c_s and slot opp(s) at x + c_s form the same set), so a
+// prefetch of another tile never sees a write of this one.
+#pragma once
+
+#include "lbm_step.cuh"
+
+namespace lbm {
+
+constexpr int kAsyncWarps = 8;   // warps per block
+constexpr int kAsyncStages = 2;
+
+template <int Q>
+constexpr size_t async_smem_bytes()
+{
+   return (size_t)kAsyncWarps * kAsyncStages * Q * 32 * sizeof(unsigned long long);
+}
+
+// Tiles of 32 cells: tile t covers x in [32 (t mod ntx), +32) of row t / ntx,
+// row r = y + ny z.  Divisions by a run-time d use q = umulhi64(n, m) with
+// m = ceil(2^64 / d) (exact for n, d < 2^32); d = 1 is m = 0.
+struct AsyncGeom {
+   uint32_t ntiles, ntx;
+   uint64_t m_ntx, m_ny;
+};
+
+__device__ __forceinline__ uint32_t div_magic(uint32_t n, uint32_t d, uint64_t m)
+{
+   return m ? (uint32_t)__umul64hi((uint64_t)n, m) : n;
+}
+
+__device__ __forceinline__ void tile_cell(const KParams& p, const AsyncGeom& ag, uint32_t t, int lane,
+                                          CellIndex& ci)
+{
+   const uint32_t row = div_magic(t, ag.ntx, ag.m_ntx);
+   const int x = (int)(t - row * ag.ntx) * 32 + lane;
+   const uint32_t z = div_magic(row, (uint32_t)p.ny, ag.m_ny);
+   const int y = (int)(row - z * (uint32_t)p.ny);
+   ci.c = (int64_t)row * p.nx + x;
+   ci.dxm = (x == 0) ? p.nx - 1 : -1;
+   ci.dxp = (x == p.nx - 1) ? -(p.nx - 1) : 1;
+   ci.dym = (y == 0) ? (p.ny - 1) * p.nx : -p.nx;
+   ci.dyp = (y == p.ny - 1) ? -(p.ny - 1) * p.nx : p.nx;
+   const int nxy = p.nx * p.ny;
+   ci.dzm = (z == 0) ? (p.nz - 1) * nxy : -nxy;
+   ci.dzp = ((int)z == p.nz - 1) ? -(p.nz - 1) * nxy : nxy;
+}
+
+__device__ __forceinline__ void cp_async8(uint32_t smem, const void* g)
+{
+   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+template <int Q, int KIND>
+__device__ __forceinline__ void async_issue(const KParams& p, const AsyncGeom& ag, const unsigned long long* src,
+                                            uint32_t pb, uint32_t t, int lane, uint32_t sbuf)
+{
+   CellIndex ci;
+   tile_cell(p, ag, t, lane, ci);
+   const unsigned long long* base = src + ci.c;
+#pragma unroll
+   for (int s = 0; s < Q; s++)
+      cp_async8(sbuf + (uint32_t)(s * 32 + lane) * 8u, slot_ptr(base, pb, read_access<Q, KIND, false>(ci, 0u, s)));
+}
+
+template <int Q, int KIND>
+__global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KParams p, const AsyncGeom ag,
+                                                                      const unsigned long long* src,
+                                                                      unsigned long long* dst)
+{
+   extern __shared__ __align__(16) unsigned long long async_smem[];
+   const int lane = threadIdx.x & 31;
+   const int warp = threadIdx.x >> 5;
+   const uint32_t nw = gridDim.x * kAsyncWarps;
+   uint32_t t = blockIdx.x * kAsyncWarps + warp;
+   if (t >= ag.ntiles) return;
+   const uint32_t pb = (uint32_t)p.plane * 8u;
+   unsigned long long* mine = async_smem + (size_t)warp * kAsyncStages * Q * 32;
+   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
+   constexpr uint32_t kStageBytes = Q * 32 * 8;
+   async_issue<Q, KIND>(p, ag, src, pb, t, lane, sbase);
+   cp_async_commit();
+   int stage = 0;
+   for (;;) {
+      const uint32_t next = t + nw;
+      if (next < ag.ntiles) async_issue<Q, KIND>(p, ag, src, pb, next, lane, sbase + (stage ^ 1) * kStageBytes);
+      cp_async_commit();
+      cp_async_wait_prev();
+      uint64_t bits[Q];
+      const unsigned long long* cur = mine + stage * Q * 32;
+#pragma unroll
+      for (int s = 0; s < Q; s++) bits[s] = cur[s * 32 + lane];
+      collide_f64x<Q>(bits, p);
+      CellIndex ci;
+      tile_cell(p, ag, t, lane, ci);
+      unsigned long long* d = dst + ci.c;
+#pragma unroll
+      for (int s = 0; s < Q; s++) *slot_ptr(d, pb, write_access<Q, KIND, false>(ci, 0u, s)) = bits[s];
+      if (next >= ag.ntiles) break;
+      t = next;
+      stage ^= 1;
+   }
+}
+
+inline AsyncGeom async_geom(int nx, int ny, int nz)
+{
+   AsyncGeom g;
+   g.ntx = (uint32_t)(nx / 32);
+   g.ntiles = g.ntx * (uint32_t)ny * (uint32_t)nz;
+   g.m_ntx = g.ntx == 1 ? 0 : (~0ull / g.ntx) + 1;
+   g.m_ny = ny == 1 ? 0 : (~0ull / (uint64_t)ny) + 1;
+   return g;
+}
+
+// Persistent grid: as many blocks as fit on the device at once (queried once
+// per device and kernel; the shared-memory opt-in is set at the same time).
+template <int Q, int KIND>
+cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src, void* dst, cudaStream_t stream)
+{
+   static int grid_of_device[64] = {0};
+   int dev = 0;
+   cudaError_t e = cudaGetDevice(&dev);
+   if (e != cudaSuccess) return e;
+   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+   auto kern = step_async_kernel<Q, KIND>;
+   constexpr size_t smem = async_smem_bytes<Q>();
+   if (grid_of_device[dev] == 0) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      int per_sm = 0, nsm = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kAsyncWarps * 32, smem);
+      if (e != cudaSuccess) return e;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      if (per_sm < 1) return cudaErrorInvalidConfiguration;
+      grid_of_device[dev] = per_sm * nsm;
+   }
+   const uint32_t need = (ag.ntiles + kAsyncWarps - 1) / kAsyncWarps;
+   const unsigned grid = (unsigned)(need < (uint32_t)grid_of_device[dev] ? need : (uint32_t)grid_of_device[dev]);
+   kern<<<grid, kAsyncWarps * 32, smem, stream>>>(p, ag, static_cast<const unsigned long long*>(src),
+                                                  static_cast<unsigned long long*>(dst));
+   return cudaGetLastError();
+}
+
+}  // namespace lbm

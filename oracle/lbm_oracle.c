@@ -8,7 +8,8 @@
  * It restates, in plain C with the reference's own data structures, the
  * single-rank CPU path of lbmminiapp:
  *
- *   - fluid-only compact storage with an int64 adjacency list built with the
+ *   - fluid-only compact storage with an adjacency list (int32 like the
+ *     reference while Q * nFluid fits, int64 beyond) built with the
  *     semantics of GeometryAAAB::setupAdjacency
  *     (src/geometries/GeometryAAAB.cpp:18-124): neighbour x+c_s for AB push,
  *     x-c_s for AA and AB pull (:44-55); a wall or out-of-box neighbour maps
