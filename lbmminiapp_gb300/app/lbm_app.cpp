@@ -9,7 +9,8 @@
 // periodic in x only as on one rank), runs AA or AB push / pull, and prints
 // the reference's lines: the input echo, fluid-point count, MFEUPS / MFLUPS
 // (src/propagation/Propagation.cpp:200-212) and the centre-line Poiseuille
-// check (src/propagation/Propagation.cpp:164-197).
+// check (src/propagation/Propagation.cpp:164-197); with "writevtk 1" it
+// writes outs.00000.vtk like the reference.
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -66,6 +67,37 @@ bool read_input(const char* path, Params& p)
          p.arithmetic = val == "f64" ? LBM_ARITH_F64 : val == "f64x" ? LBM_ARITH_F64X : LBM_ARITH_AUTO;
    }
    return true;
+}
+
+// Propagation::writeVTK (src/propagation/Propagation.cpp:36-161) on one rank:
+// outs.00000.vtk with rho, point id, velocity and node coordinates, x fastest,
+// default stream formatting.  Non-fluid points: rho 0, velocity 0 0 0, id
+// LAT_PT_WALL (-10); fluid points are numbered in x-fastest order.
+bool write_vtk(const char* path, const int dims[3], const std::vector<uint8_t>& solid,
+               const std::vector<double>& rho, const std::vector<double>& u)
+{
+   std::ofstream f(path);
+   if (!f) return false;
+   const size_t n = solid.size();
+   f << "# vtk DataFile Version 3.0" << "\n" << "Placeholder" << "\n" << "ASCII" << "\n"
+     << "DATASET STRUCTURED_POINTS" << "\n"
+     << "DIMENSIONS " << dims[0] << " " << dims[1] << " " << dims[2] << "\n"
+     << "ORIGIN 0 0 0" << "\n" << "SPACING 1 1 1" << "\n" << "POINT_DATA " << n << "\n";
+   f << "SCALARS rho double" << "\n" << "LOOKUP_TABLE default" << "\n";
+   for (size_t c = 0; c < n; c++) f << (solid[c] ? 0.0 : rho[c]) << "\n";
+   f << "SCALARS id int" << "\n" << "LOOKUP_TABLE default" << "\n";
+   long long fid = 0;
+   for (size_t c = 0; c < n; c++) f << (solid[c] ? -10LL : fid++) << "\n";
+   f << "VECTORS velocity double" << "\n";
+   for (size_t c = 0; c < n; c++) {
+      if (solid[c]) f << 0.0 << " " << 0.0 << " " << 0.0 << "\n";
+      else f << u[c] << " " << u[n + c] << " " << u[2 * n + c] << "\n";
+   }
+   f << "VECTORS nodes int" << "\n";
+   for (int k = 0; k < dims[2]; k++)
+      for (int j = 0; j < dims[1]; j++)
+         for (int i = 0; i < dims[0]; i++) f << i << " " << j << " " << k << "\n";
+   return (bool)f;
 }
 
 int die(lbm_handle* h, lbm_status s, const char* what)
@@ -151,6 +183,11 @@ int main(int argc, char** argv)
                 << std::endl;
       std::printf("Centre-line velocity %.17g (Poiseuille %.17g)\n", vel, expected);
       std::fflush(stdout);
+   }
+   if (p.writeVtk && !write_vtk("outs.00000.vtk", dims, solid, rho, u)) {
+      std::fprintf(stderr, "cannot write outs.00000.vtk\n");
+      lbm_destroy(h);
+      return 1;
    }
    lbm_destroy(h);
    const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - tStart).count();

@@ -125,7 +125,18 @@ class Propagation:
         self.elapsed = time.perf_counter() - t0
         self.printMFLUPS(self.elapsed)
         self.rho, self.u = self.sim.macros()
-        return self.checkResult(steps if self.pattern == "aa" else steps - 1)
+        read_step = steps if self.pattern == "aa" else steps - 1
+        ok = self.checkResult(read_step)
+        if self.parameters.writeVtk:
+            self.writeVTK(read_step)
+        return ok
+
+    def writeVTK(self, currentStep, path="outs.00000.vtk"):
+        """src/propagation/Propagation.cpp:36-161 (single rank: outs.00000.vtk
+        in the working directory), from the readouts of the last run."""
+        from .vtk import write_vtk
+        write_vtk(path, self.rho, self.u, self.solid)
+        return path
 
     def getRho(self, i, j, k):
         return float(self.rho[k, j, i])

@@ -77,6 +77,35 @@ def make_cylinder(tmpdir):
         print(f"{name}: nfluid {out['nfluid']}")
 
 
+# The reference's VTK output (Propagation::writeVTK, src/propagation/
+# Propagation.cpp:36-161) of a size-1 AA Unroll cylinder run: the header and
+# the rho and velocity sections as the reference printed them (its "id"
+# section numbers fluid points in the reference's own sorted order, and
+# "nodes" is the index grid, so neither is kept).
+VTK_CASE = "cylinder_s1_aa_unroll_vtk"
+VTK_KEYS = dict(propPattern=1, pull=0, unroll=1)
+
+
+def make_vtk(tmpdir):
+    import gzip
+    import os
+    inp = cylinder_input(Path(tmpdir) / f"{VTK_CASE}.txt", **VTK_KEYS, size=1.0)
+    inp.write_text(inp.read_text().replace("writevtk 0", "writevtk 1"))
+    cwd = os.getcwd()
+    os.chdir(tmpdir)
+    try:
+        ref.app_run(19, inp, omega=1.0, gx=1e-6)
+    finally:
+        os.chdir(cwd)
+    lines = (Path(tmpdir) / "outs.00000.vtk").read_text().split("\n")
+    i_id, i_vel, i_nodes = (lines.index(k) for k in ("SCALARS id int", "VECTORS velocity double",
+                                                     "VECTORS nodes int"))
+    keep = lines[:i_id] + lines[i_vel:i_nodes]
+    with gzip.open(HERE / f"{VTK_CASE}.txt.gz", "wt") as f:
+        f.write("\n".join(keep) + "\n")
+    print(f"{VTK_CASE}: {len(keep)} lines")
+
+
 def main():
     if not ref.available():
         sys.exit("reference harness unavailable (oracle/build_ref.sh needs the reference sources)")
@@ -90,6 +119,8 @@ def main():
     import tempfile
     with tempfile.TemporaryDirectory() as tmp:
         make_cylinder(tmp)
+    with tempfile.TemporaryDirectory() as tmp:
+        make_vtk(tmp)
 
 
 if __name__ == "__main__":

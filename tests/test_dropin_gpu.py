@@ -59,3 +59,49 @@ def test_cpp_driver_cylinder(gpu, tmp_path, name):
     cj, ck = (int(dims[1]) - 1) // 2, (int(dims[2]) - 1) // 2
     ref_vel = float(g["u_plane"][0, ck, cj])
     assert abs(vel - ref_vel) <= 1e-10 * abs(ref_vel)
+
+
+def _vtk_golden():
+    import gzip
+    text = gzip.open(ROOT / "tests" / "golden" / "cylinder_s1_aa_unroll_vtk.txt.gz", "rt").read().split("\n")
+    return text
+
+
+def _vtk_input(path, extra=""):
+    path.write_text("simulationSize 1.0\npropPattern 1\npull 0\nunroll 1\ndensityChange 0.01\nwritevtk 1\n"
+                    "timesteps 100\n" + extra)
+    return path
+
+
+def _check_vtk_against_reference(path):
+    """Header, rho and velocity sections: the same text as the reference's
+    outs.00000.vtk; ids: LAT_PT_WALL at the reference's walls (rho 0 there)."""
+    golden = _vtk_golden()
+    ours = Path(path).read_text().split("\n")
+    i_id, i_vel, i_nodes = (ours.index(k) for k in ("SCALARS id int", "VECTORS velocity double",
+                                                    "VECTORS nodes int"))
+    assert ours[:i_id] + ours[i_vel:i_nodes] == golden[:-1]
+    ids = np.array(ours[i_id + 2:i_vel], dtype=np.int64)
+    rho = golden[10:i_id]
+    walls = np.array([r == "0" for r in rho])
+    assert np.array_equal(ids < 0, walls) and (ids[walls] == -10).all()
+    assert np.array_equal(ids[~walls], np.arange((~walls).sum()))
+
+
+def test_reference_api_writes_reference_vtk(gpu, tmp_path, monkeypatch):
+    """writevtk 1 through the Python mirror, exact FP64 arithmetic: the VTK
+    text equals the reference's own output of the same run."""
+    from lbmminiapp_gb300 import reference_api
+    inp = _vtk_input(tmp_path / "in.txt", "arithmetic f64\n")
+    monkeypatch.chdir(tmp_path)
+    reference_api.main(str(inp), out=lambda s: None)
+    _check_vtk_against_reference(tmp_path / "outs.00000.vtk")
+
+
+def test_cpp_driver_writes_reference_vtk(gpu, tmp_path):
+    from lbmminiapp_gb300 import build
+    app = build.build_app() if not build.APP.exists() else build.APP
+    inp = _vtk_input(tmp_path / "in.txt", "arithmetic f64\n")
+    out = subprocess.run([str(app), str(inp)], capture_output=True, text=True, timeout=300, cwd=tmp_path)
+    assert out.returncode == 0, out.stderr
+    _check_vtk_against_reference(tmp_path / "outs.00000.vtk")
