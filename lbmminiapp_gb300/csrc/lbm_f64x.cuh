@@ -6,10 +6,13 @@
 // HBM roofline.  This path keeps the populations
 // in FP64 memory (the reference's Pdf buffers) but:
 //
-//  * splits each loaded double into an unevaluated float pair (h, l) with
-//    integer operations only: h is the double truncated to 24 significant
-//    bits, l the remaining bits rounded to 23 (|f - (h + l)| <= 2^-48 |f|);
-//  * evaluates rho, j = sum c f, u, the equilibrium and the BGK/Guo update in
+//  * splits each loaded double into an unevaluated float pair (h, l): h is
+//    the double truncated to 24 significant bits (integer operations), l the
+//    remaining 29 mantissa bits rounded to 24 by an integer-to-float
+//    conversion and scaled (|f - (h + l)| <= 2^-48 |f|);
+//  * sums rho and j = sum c f exactly from 64-bit fixed-point images of the
+//    doubles (integer adds);
+//  * evaluates u, the equilibrium and the BGK/Guo update in
 //    double-float arithmetic built from the error-free transformations
 //    TwoSum (Knuth), Fast2Sum (Dekker 1971) and the FMA two-product, as used
 //    in double-double libraries (Hida, Li & Bailey, "Library for double-double
@@ -17,7 +20,7 @@
 //  * rebuilds the 64-bit pattern of the result (the double nearest to h + l)
 //    with integer operations and one float-to-int conversion.
 //
-// The fast path covers positive populations in [2^-75, 1), the only values a
+// The fast path covers positive populations in [2^-32, 1), the only values a
 // physical state holds (with further bounds on the rest population and the
 // velocity, checked per cell).  A cell whose inputs or results fall outside
 // them is recomputed with the exact IEEE double collision, so any state is
@@ -125,7 +128,7 @@ __host__ __device__ __forceinline__ float frcp(float a)
 #endif
 }
 
-// Low 32 bits of ((hi:lo) << n), 0 <= n < 32.
+// High 32 bits of ((hi:lo) << n), 0 <= n < 32.
 __host__ __device__ __forceinline__ uint32_t funnel_l(uint32_t lo, uint32_t hi, uint32_t n)
 {
 #ifdef __CUDA_ARCH__
@@ -133,6 +136,37 @@ __host__ __device__ __forceinline__ uint32_t funnel_l(uint32_t lo, uint32_t hi, 
 #else
    const uint64_t v = ((uint64_t)hi << 32) | lo;
    return (uint32_t)((v << n) >> 32);
+#endif
+}
+
+// Low 32 bits of ((hi:lo) >> n), 0 <= n < 32.
+__host__ __device__ __forceinline__ uint32_t funnel_r(uint32_t lo, uint32_t hi, uint32_t n)
+{
+#ifdef __CUDA_ARCH__
+   return __funnelshift_r(lo, hi, n);
+#else
+   const uint64_t v = ((uint64_t)hi << 32) | lo;
+   return (uint32_t)(v >> n);
+#endif
+}
+
+__host__ __device__ __forceinline__ float i2f_rn(int32_t i)
+{
+#ifdef __CUDA_ARCH__
+   return __int2float_rn(i);
+#else
+   volatile float r = (float)i;
+   return r;
+#endif
+}
+
+__host__ __device__ __forceinline__ float u2f_rn(uint32_t u)
+{
+#ifdef __CUDA_ARCH__
+   return __uint2float_rn(u);
+#else
+   volatile float r = (float)u;
+   return r;
 #endif
 }
 
@@ -207,56 +241,89 @@ __host__ __device__ __forceinline__ df df_from_double(double d)
 }
 
 // ------------------------------------------------ double <-> float pair
-// Fast-path range of the double bit patterns: positive, 2^-75 <= f < 1.
-constexpr uint32_t kHiMin = (uint32_t)(1023 - 75) << 20;   // high word of 2^-75
+// Fast-path range of the double bit patterns: positive, 2^-32 <= f < 1.
+constexpr uint32_t kHiMin = (uint32_t)(1023 - 32) << 20;   // high word of 2^-32
 constexpr uint32_t kHiMax = (uint32_t)1023 << 20;          // high word of 1.0 (excluded)
 
-// Split a double (given as its 64-bit pattern, in range) into (h, l).
-//   t  = bits 59..28 of the pattern: the low 8 exponent bits above the top
-//        23 mantissa bits; adding 2^30 re-biases exponent 1023 to 127
-//        (E - 896) within the 8-bit field, valid for E in [897, 1150].
-//   l  = the remaining 29 mantissa bits rounded to nearest 23 (a float with
-//        exponent e(h) - 23 and its implicit 1 subtracted, exact by Sterbenz;
-//        a carry out of the 23 bits moves into that float's exponent, which
-//        is still the correctly rounded value).  |f - (h + l)| <= 2^-48 |f|.
+// Split a positive double in range (given as its 64-bit pattern) into (h, l).
+//   h  = bits 60..29 of the pattern (the low 9 exponent bits above the top
+//        23 mantissa bits) plus 2^30, masked to 31 bits: exponent E
+//        re-biased to E - 896 in the float's 8-bit field, valid for E in
+//        [897, 1150];
+//   l  = the low 29 mantissa bits as an integer, rounded to nearest 24 bits
+//        by the conversion and scaled by 2^(e(h) - 52) (a power of two, no
+//        underflow for e(h) >= -74).  |f - (h + l)| <= 2^-48 |f|.
 __host__ __device__ __forceinline__ df split(uint64_t bits)
 {
    const uint32_t lo = (uint32_t)bits, hi = (uint32_t)(bits >> 32);
-   const uint32_t t = funnel_l(lo, hi, 3);
-   const uint32_t hb = ((t + 0x40000000u) & 0x7FFFFFFFu) | (hi & 0x80000000u);
-   const uint32_t a = hb - (23u << 23);
-   const uint32_t mb = a & 0xFF800000u;
-   const uint32_t m24 = (lo >> 5) & 0x00FFFFFFu;          // 23 bits + the rounding bit
-   const uint32_t xb = mb + ((m24 + 1u) >> 1);             // round half up
-   return {bitsf(hb), fsub(bitsf(xb), bitsf(mb))};
+   const uint32_t hb = (funnel_l(lo, hi, 3) + 0x40000000u) & 0x7FFFFFFFu;
+   const float scale = bitsf((hb & 0x7F800000u) - (52u << 23));
+   return {bitsf(hb), fmul(u2f_rn(lo & 0x1FFFFFFFu), scale)};
 }
 
-__host__ __device__ __forceinline__ int32_t f2i_rn(float x)
+// Fixed-point image of a positive double f in [2^-32, 1) for the moment
+// sums: floor(f * 2^53) as a 64-bit integer, the 53-bit mantissa (with its
+// implicit bit) shifted right by k = 1022 - E, in [0, 31] for that range.
+// Sums of these images are exact; the truncation loses less than 2^-53 per
+// population (its mean, half a unit, is added back to rho).
+__host__ __device__ __forceinline__ uint64_t fixed53(uint64_t bits)
+{
+   const uint32_t lo = (uint32_t)bits, hi = (uint32_t)(bits >> 32);
+   const uint32_t mh = (hi & 0x000FFFFFu) | 0x00100000u;
+   const uint32_t k = 1022u - (hi >> 20);
+   return ((uint64_t)(mh >> k) << 32) | funnel_r(lo, mh, k);
+}
+
+// Float pair of v * 2^-53 for a signed 64-bit v with |v| < 2^54: the top
+// part v >> 30 is an exact float, the low 30 bits are rounded to 24
+// (absolute error <= 2^-48).  Not normalised: h may be 0 or below l.
+__host__ __device__ __forceinline__ df fixed53_to_pair(int64_t v)
+{
+   const uint32_t lo = (uint32_t)v, hi = (uint32_t)((uint64_t)v >> 32);
+   const int32_t top = (int32_t)funnel_l(lo, hi, 2);        // v >> 30 (arithmetic)
+   return {fmul(i2f_rn(top), 0x1p-23f), fmul(u2f_rn(lo & 0x3FFFFFFFu), 0x1p-53f)};
+}
+
+// Non-negative float to unsigned int, rounded to nearest even.
+__host__ __device__ __forceinline__ uint32_t f2u_rn(float x)
 {
 #ifdef __CUDA_ARCH__
-   return __float2int_rn(x);
+   return __float2uint_rn(x);
 #else
-   return (int32_t)std::nearbyint(x);
+   return (uint32_t)std::nearbyint(x);
 #endif
 }
 
-// Double pattern of h + l (positive) with the output range check folded in:
-//   S  = h + l rounded toward zero (so the remainder E >= 0 stays inside S's
-//        binade), E = the remainder (exact);
-//   N  = E in units of one double ulp of S, an exact float below 2^29,
-//        rounded to the nearest integer;
-//   the pattern of S as a double plus N: the double nearest to h + l.
-// ok becomes false unless 2^-75 <= S < 1.
-__host__ __device__ __forceinline__ uint64_t join_checked(df v, bool& ok)
+// Running check of the result patterns of one cell: the largest
+// sb - pattern(2^-75) as unsigned (a result below 2^-75 wraps around, a
+// negative or NaN one lands above the bound).
+struct JoinRange {
+   uint32_t worst = 0u;
+   __host__ __device__ __forceinline__ void add(uint32_t sb)
+   {
+      const uint32_t d = sb - 0x1A000000u;
+      worst = worst > d ? worst : d;
+   }
+   // 2^-75 <= S < 1 for every result
+   __host__ __device__ __forceinline__ bool ok() const { return worst < 0x3F800000u - 0x1A000000u; }
+};
+
+// Double pattern of h + l (positive):
+//   S  = h + l rounded toward zero, E = the remainder h + l - S (exact, >= 0);
+//   N  = E in units of one double ulp of S, an exact float below
+//        2^29 - 2^5 (E < ulp_float(S)), rounded to the nearest integer;
+//   the pattern of S as a double plus N: the double nearest to h + l.  S's
+//   double pattern has 29 zero low bits, so N goes in with an OR.
+// S's pattern goes into `range`; the result is valid when range.ok().
+__host__ __device__ __forceinline__ uint64_t join(df v, JoinRange& range)
 {
    const float S = fadd_rz(v.h, v.l);
    const float E = fsub(v.l, fsub(S, v.h));
    const uint32_t sb = fbits(S);
-   ok = ok && (sb - 0x1A000000u) < (0x3F800000u - 0x1A000000u);
+   range.add(sb);
    const float scale = bitsf(0x99000000u - (sb & 0x7F800000u));  // 2^(52 - e(S))
-   const int32_t n = f2i_rn(fmul(E, scale));
-   const uint64_t d0 = ((uint64_t)sb << 29) + ((uint64_t)0x38000000u << 32);
-   return d0 + (uint64_t)(int64_t)n;
+   const uint32_t n = f2u_rn(fmul(E, scale));
+   return (((uint64_t)sb << 29) + ((uint64_t)0x38000000u << 32)) | n;
 }
 
 __host__ __device__ __forceinline__ double as_double(uint64_t b)
@@ -316,9 +383,8 @@ constexpr uint32_t kHiQuarter = (uint32_t)(1023 - 2) << 20;   // 0.25
 // The fast-path collision on one cell.  bits[] holds the Q input patterns in
 // direction order and receives the Q output patterns.  Returns false (leaving
 // bits[] untouched) when the cell must take the exact path:
-//   * inputs: rest population in [0.25, 1), the others in [2^-75, 0.25) --
-//     (and 2^-75 below) so rho's running sum, started at the rest population, always has an
-//     exponent at least that of the next term (Fast2Sum is exact);
+//   * inputs: rest population in [0.25, 1), the others in [2^-32, 0.25), and
+//     rho < 2;
 //   * |3 v_d| < 0.3: |c.u| stays well below 1 - uu/2, so the pair sums
 //     (1 - uu/2 + cu^2/2) +- cu keep their larger operand first;
 //   * outputs inside [2^-75, 1).
@@ -346,61 +412,34 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
 #pragma unroll
    for (int s = 0; s < Q; s++) f[s] = split(bits[s]);
 
-   // rho = f_rest + sum of the rest (Fast2Sum chain, exact by the range check);
-   // the low word is folded back every 6 terms so it stays near ulp(rho).
-   float rh = f[R].h, rl = f[R].l;
+   // rho and j = sum c_s f_s from the exact sums of the fixed-point images
+   // floor(f * 2^53); rho < 2 is checked (rho's top word below 2^22).
+   uint64_t X[Q];
 #pragma unroll
-   for (int s = 0; s < Q; s++) {
-      if (s == R) continue;
-      const float t = fadd(rh, f[s].h);
-      rl = fadd(rl, fadd(fsub(f[s].h, fsub(t, rh)), f[s].l));
-      rh = t;
-      if (s % 6 == 5) {
-         const df n = fast_two_sum(rh, rl);
-         rh = n.h;
-         rl = n.l;
-      }
-   }
-   const df rho = fast_two_sum(rh, rl);
-
-   // j = sum over pairs of c_s (f_s - f_opp(s)), differences by TwoSum
-   df D[NP];
+   for (int s = 0; s < Q; s++) X[s] = fixed53(bits[s]);
+   uint64_t rho_x = (uint64_t)(Q / 2);   // mean truncation loss, half a unit per population
 #pragma unroll
-   for (int q = 0; q < NP; q++) {
-      const int s = pair_dir(Q, q), o = lat_opp(Q, s);
-      const df t = two_sum(f[s].h, -f[o].h);
-      D[q] = {t.h, fadd(t.l, fsub(f[s].l, f[o].l))};
-   }
+   for (int s = 0; s < Q; s++) rho_x += X[s];
+   if ((rho_x >> 32) >= (1u << 22)) return false;
    df j[3];
 #pragma unroll
    for (int d = 0; d < 3; d++) {
-      float jh = 0.f, jl = 0.f;
-      bool first = true;
+      int64_t jx = 0;
 #pragma unroll
-      for (int q = 0; q < NP; q++) {
-         const int c = lat_c(Q, pair_dir(Q, q), d);
-         if (c == 0) continue;
-         const float th = c > 0 ? D[q].h : -D[q].h;
-         const float tl = c > 0 ? D[q].l : -D[q].l;
-         if (first) {
-            jh = th;
-            jl = tl;
-            first = false;
-         } else {
-            const df t = two_sum(jh, th);
-            jh = t.h;
-            jl = fadd(jl, fadd(t.l, tl));
-            if (q % 4 == 3) {
-               const df n = fast_two_sum(jh, jl);
-               jh = n.h;
-               jl = n.l;
-            }
-         }
+      for (int s = 0; s < Q; s++) {
+         const int c = lat_c(Q, s, d);
+         if (c > 0) jx += (int64_t)X[s];
+         if (c < 0) jx -= (int64_t)X[s];
       }
-      j[d] = fast_two_sum(jh, jl);
+      // Fast2Sum is exact here: t.h is 0 or a multiple of 2^-23 above |t.l|.
+      const df t = fixed53_to_pair(jx);
+      j[d] = fast_two_sum(t.h, t.l);
    }
+   // rho >= 1/4 (the rest population alone): Fast2Sum normalises the pair.
+   const df rho0 = fixed53_to_pair((int64_t)rho_x);
+   const df rho = fast_two_sum(rho0.h, rho0.l);
 
-   // v = (j + F/2) / rho
+   // v = (j + F/2) / rho, left unnormalised (p + e); 3v normalised
    const float r0 = frcp(rho.h);
    float e = ffma(-rho.h, r0, 1.0f);
    e = ffma(-rho.l, r0, e);
@@ -408,17 +447,24 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
    df v[3], v3[3];
 #pragma unroll
    for (int d = 0; d < 3; d++) {
-      const df jf = df_add(j[d], {0.5f * k.F[d].h, 0.5f * k.F[d].l});
-      v[d] = df_mul(jf, inv);
+      const df jf = FORCE ? df_add(j[d], {0.5f * k.F[d].h, 0.5f * k.F[d].l}) : j[d];
+      v[d] = df_mul_u(jf, inv);
       const float p = fmul(3.0f, v[d].h);
       v3[d] = fast_two_sum(p, ffma(3.0f, v[d].h, -p) + 3.0f * v[d].l);
    }
    if (!(fabsf(v3[0].h) < 0.3f && fabsf(v3[1].h) < 0.3f && fabsf(v3[2].h) < 0.3f)) return false;
-   // uu = 3 v.v
-   df uu = df_mul_u(v3[0], v[0]);
-   uu = df_add(uu, df_mul_u(v3[1], v[1]));
-   uu = df_add(uu, df_mul_u(v3[2], v[2]));
-   const df base = df_add_fast({1.0f, 0.0f}, {-0.5f * uu.h, -0.5f * uu.l});
+   // base = 1 - uu/2 with uu = 3 v.v, as a Fast2Sum chain from 1 (each
+   // term 3 v_d^2 / 2 < 0.045 stays below the running value); left
+   // unnormalised (its low part is a few ulps of its high part at most).
+   df base;
+   {
+      const df p0 = df_mul_u(v3[0], v[0]), p1 = df_mul_u(v3[1], v[1]), p2 = df_mul_u(v3[2], v[2]);
+      const df b0 = fast_two_sum(1.0f, -0.5f * p0.h);
+      const df b1 = fast_two_sum(b0.h, -0.5f * p1.h);
+      const df b2 = fast_two_sum(b1.h, -0.5f * p2.h);
+      const float lows = ffma(-0.5f, p2.l, ffma(-0.5f, p1.l, ffma(-0.5f, p0.l, fadd(b0.l, b1.l))));
+      base = {b2.h, fadd(b2.l, lows)};
+   }
    // fu = 3 F.v (float pair; zero without a force)
    df fu = {0.f, 0.f};
    if (FORCE) {
@@ -429,13 +475,13 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
 
    df owr[4];
 #pragma unroll
-   for (int cls = 0; cls < 4; cls++) owr[cls] = df_mul(k.ow[cls], rho);
+   for (int cls = 0; cls < 4; cls++) owr[cls] = df_mul_u(k.ow[cls], rho);
 
    // Results are written back only after every output passed its check (a
    // fallback must still see the original inputs).
    uint64_t res[Q - 1];
    uint64_t rest_bits;
-   bool ok = true;
+   JoinRange range;
    // rest direction: P = base
    {
       const df A = df_mul_u(owr[0], base);
@@ -448,7 +494,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
          const df t2 = two_sum(out.h, -fr.h);
          out = {t2.h, fadd(t2.l, fsub(out.l, fr.l))};
       }
-      rest_bits = join_checked(out, ok);
+      rest_bits = join(out, range);
    }
 #pragma unroll
    for (int q = 0; q < NP; q++) {
@@ -495,7 +541,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
             const df t2 = two_sum(out.h, fr.h);
             out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fadd(k.Kf[s].l, sym.l))))};
          }
-         res[q] = join_checked(out, ok);
+         res[q] = join(out, range);
       }
       {
          const df tm = fast_two_sum(A.h, -B.h);
@@ -507,10 +553,10 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
             const df t2 = two_sum(out.h, fr.h);
             out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fsub(sym.l, k.Kf[s].l))))};
          }
-         res[NP + q] = join_checked(out, ok);
+         res[NP + q] = join(out, range);
       }
    }
-   if (!ok) return false;
+   if (!range.ok()) return false;
 #pragma unroll
    for (int q = 0; q < NP; q++) {
       const int s = pair_dir(Q, q);

@@ -67,16 +67,20 @@ __device__ __forceinline__ void cp_async8(uint32_t smem, const void* g)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
+// Addresses: plane base (slot * plane, the same for every tile) plus a
+// 32-bit cell index (fewer than 2^31 cells; the periodic wrap keeps
+// neighbour indices inside the box).
 template <int Q, int KIND>
-__device__ __forceinline__ void async_issue(const KParams& p, const AsyncGeom& ag, const unsigned long long* src,
-                                            uint32_t pb, uint32_t t, int lane, uint32_t sbuf)
+__device__ __forceinline__ void async_issue(const unsigned long long* src, int64_t plane, const CellIndex& ci,
+                                            int lane, uint32_t sbuf)
 {
-   CellIndex ci;
-   tile_cell(p, ag, t, lane, ci);
-   const unsigned long long* base = src + ci.c;
+   const uint32_t c = (uint32_t)ci.c;
 #pragma unroll
-   for (int s = 0; s < Q; s++)
-      cp_async8(sbuf + (uint32_t)(s * 32 + lane) * 8u, slot_ptr(base, pb, read_access<Q, KIND, false>(ci, 0u, s)));
+   for (int s = 0; s < Q; s++) {
+      const Access a = read_access<Q, KIND, false>(ci, 0u, s);
+      const unsigned long long* plane_base = src + a.slot * plane;
+      cp_async8(sbuf + (uint32_t)(s * 32 + lane) * 8u, plane_base + (c + (uint32_t)a.off));
+   }
 }
 
 template <int Q, int KIND>
@@ -85,35 +89,47 @@ __global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KPar
                                                                       unsigned long long* dst)
 {
    extern __shared__ __align__(16) unsigned long long async_smem[];
+   constexpr bool kInPlace = KIND == K_AA_EVEN || KIND == K_AA_ODD;
+   // AA runs in place on one buffer (the caller passes src == dst).
+   unsigned long long* out = kInPlace ? const_cast<unsigned long long*>(src) : dst;
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
    const uint32_t nw = gridDim.x * kAsyncWarps;
    uint32_t t = blockIdx.x * kAsyncWarps + warp;
    if (t >= ag.ntiles) return;
-   const uint32_t pb = (uint32_t)p.plane * 8u;
+   const int64_t plane = p.plane;
    unsigned long long* mine = async_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 8;
-   async_issue<Q, KIND>(p, ag, src, pb, t, lane, sbase);
+   CellIndex cur;
+   tile_cell(p, ag, t, lane, cur);
+   async_issue<Q, KIND>(src, plane, cur, lane, sbase);
    cp_async_commit();
    int stage = 0;
    for (;;) {
       const uint32_t next = t + nw;
-      if (next < ag.ntiles) async_issue<Q, KIND>(p, ag, src, pb, next, lane, sbase + (stage ^ 1) * kStageBytes);
+      CellIndex nxt = cur;
+      if (next < ag.ntiles) {
+         tile_cell(p, ag, next, lane, nxt);
+         async_issue<Q, KIND>(src, plane, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
+      }
       cp_async_commit();
       cp_async_wait_prev();
       uint64_t bits[Q];
-      const unsigned long long* cur = mine + stage * Q * 32;
+      const unsigned long long* sm = mine + stage * Q * 32;
 #pragma unroll
-      for (int s = 0; s < Q; s++) bits[s] = cur[s * 32 + lane];
+      for (int s = 0; s < Q; s++) bits[s] = sm[s * 32 + lane];
       collide_f64x<Q>(bits, p);
-      CellIndex ci;
-      tile_cell(p, ag, t, lane, ci);
-      unsigned long long* d = dst + ci.c;
+      const uint32_t c = (uint32_t)cur.c;
 #pragma unroll
-      for (int s = 0; s < Q; s++) *slot_ptr(d, pb, write_access<Q, KIND, false>(ci, 0u, s)) = bits[s];
+      for (int s = 0; s < Q; s++) {
+         const Access a = write_access<Q, KIND, false>(cur, 0u, s);
+         unsigned long long* plane_base = out + a.slot * plane;
+         plane_base[c + (uint32_t)a.off] = bits[s];
+      }
       if (next >= ag.ntiles) break;
       t = next;
+      cur = nxt;
       stage ^= 1;
    }
 }
