@@ -213,6 +213,56 @@ def traffic_per_launch():
     return d.get("bytes_per_launch_512")
 
 
+def cylinder_benchmark(device, size=8.0, steps=20):
+    """The reference's own published benchmark workload: the size-8 cylinder
+    (8,913,408 fluid points, src/geometries/Geometry.cpp:59-71,112-140),
+    D3Q19, FP64, gravity-driven flow from rest, x periodic.  MLUPS per fluid
+    point for AA, AB push and AB pull, through the compact fluid-only layout
+    (the reference's own buffers and adjacency list) and the dense layout
+    (link words), both with F64X arithmetic; CUDA events around `steps`
+    steps after 2 warm-up steps.  The reference publishes 457-1017 MLUPS for
+    this workload on one Intel Xe-HP tile."""
+    import torch
+    import lbmminiapp_gb300 as lbm
+    from lbmminiapp_gb300 import sparse
+    dims, solid = lbm.cylinder(size)
+    nx, ny, nz = dims
+    out = {"workload": f"cylinder size {size:g}, {nx}x{ny}x{nz}, D3Q19 FP64 (F64X), omega 1, gx 1e-6",
+           "steps": steps}
+    nfluid = int((solid == 0).sum())
+    out["nfluid"] = nfluid
+    w = np.array([1 / 18] * 6 + [1 / 36] * 12 + [1 / 3])
+
+    def timed(run):
+        run(2)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        run(steps)
+        b.record()
+        b.synchronize()
+        return round(nfluid * steps / (a.elapsed_time(b) * 1e-3) / 1e6, 1)
+
+    for pattern in ("aa", "ab_push", "ab_pull"):
+        _, adj = sparse.build_adjacency(solid, (1, 0, 0), pattern, 19)
+        f0 = torch.tensor(np.repeat(w[:, None], nfluid, axis=1), dtype=torch.float64, device="cuda")
+        bufs = [f0] if pattern == "aa" else [f0, f0.clone()]
+        with sparse.SparseKernels(adj, lattice=19, pattern=pattern, omega=1.0, force=(1e-6, 0, 0),
+                                  device=device) as k:
+            k.set_stream(torch.cuda.current_stream())
+
+            def run(n):   # n even: AA parity and the AB buffer roles are unchanged
+                k.run(bufs, n)
+            out[f"compact/{pattern}"] = timed(run)
+        del bufs, f0
+        with lbm.Simulation(nx, ny, nz, lattice=19, pattern=pattern, omega=1.0, force=(1e-6, 0, 0),
+                            periodic=(1, 0, 0), device=device) as sim:
+            sim.set_solid(solid)
+            sim.init_equilibrium(None, None)
+            out[f"dense/{pattern}"] = timed(sim.step)
+    return out
+
+
 def run_reference_arm(args, dist, rank, world):
     if rank != 0:
         return 0
@@ -364,6 +414,10 @@ def main():
             s2.close()
         del uv
 
+    cylinder = {}
+    if not args.no_variants and headline:
+        cylinder = cylinder_benchmark(local)
+
     cpu = None
     if not args.no_cpu and rank == 0:
         sample_n = 128
@@ -393,6 +447,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": e2e,
             "variants": variants,
+            "reference_benchmark": cylinder,
             "mass_per_cell_after": mass,
             "clocks": clk.summary(),
         }

@@ -207,6 +207,37 @@ lbm_status lbm_adjoint_step_f32(lbm_handle* h, const void* state, const float* l
                                 int loss_kind, const double* weight, double time_weight, double* grad_force,
                                 double* grad_porosity);
 
+/* ---- compact fluid-only layout (the reference's own buffers and adjacency).
+ * The reference keeps populations only for fluid points, direction s of fluid
+ * point i at dstrb[nFluid*s + i], and streams through the int32 adjacency list
+ * of GeometryAAAB::setupAdjacency (src/geometries/GeometryAAAB.cpp:18-124):
+ * adjacency[nFluid*s + i] is the element index of slot s at the neighbour
+ * x - c_s (AA, AB pull) or x + c_s (AB push), or nFluid*opp(s) + i for a wall.
+ * A sparse handle holds a device copy of that list and runs the reference's
+ * kernel steps on caller-owned device buffers in that layout, in any fluid
+ * order.  cfg: lattice, prop_pattern, pull, unroll, omega, force, arithmetic
+ * (AUTO/F64X or F64), device and max_device_bytes are used; storage must be
+ * LBM_STORE_F64; the grid fields are ignored.  Q * nfluid must stay below
+ * 2^31 (the reference's int32 indices); every adjacency entry must lie in
+ * [0, Q * nfluid).  Steps run asynchronously on the handle's stream. */
+typedef struct lbm_sparse_handle lbm_sparse_handle;
+/* GeometryAAAB::setupAdjacency's result as the handle's streaming map;
+ * adjacency: host, [Q][nfluid] int32. */
+lbm_status lbm_sparse_create(const lbm_config* cfg, int64_t nfluid, const int32_t* adjacency,
+                             lbm_sparse_handle** out);
+void lbm_sparse_destroy(lbm_sparse_handle* h);
+const char* lbm_sparse_last_error(const lbm_sparse_handle* h); /* never NULL */
+lbm_status lbm_sparse_set_stream(lbm_sparse_handle* h, void* stream);
+/* KernelAA::timestepEvenForce(Pdf* dstrb, int startIdx, int countIdx)
+ * (src/kernels/KernelAA.hh:28) on a compact device buffer of Q*nfluid doubles */
+lbm_status lbm_sparse_timestep_even_force(lbm_sparse_handle* h, double* dstrb, int64_t start, int64_t count);
+/* KernelAA::timestepOddForce (src/kernels/KernelAA.hh:29) */
+lbm_status lbm_sparse_timestep_odd_force(lbm_sparse_handle* h, double* dstrb, int64_t start, int64_t count);
+/* KernelAB::timestepForce(Pdf* src, Pdf* tgt, int startIdx, int countIdx)
+ * (src/kernels/KernelAB.hh:87); push or pull per cfg.pull */
+lbm_status lbm_sparse_timestep_force(lbm_sparse_handle* h, const double* src, double* tgt, int64_t start,
+                                     int64_t count);
+
 /* ---- allocation-free conservation reduction.  No counterpart in the
  * reference.  For callers that cannot allocate device memory while they run
  * (hosts that give every device byte to their own pool at start-up, drivers

@@ -80,6 +80,13 @@ _SIGNATURES = {
     "lbm_loss": (ctypes.c_int, [_P, _P, ctypes.c_int, _P, ctypes.c_double, _P]),
     "lbm_adjoint_step": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P, _P]),
     "lbm_adjoint_step_f32": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P, _P]),
+    "lbm_sparse_create": (ctypes.c_int, [ctypes.POINTER(Config), _I64, _P, ctypes.POINTER(_P)]),
+    "lbm_sparse_destroy": (None, [_P]),
+    "lbm_sparse_last_error": (ctypes.c_char_p, [_P]),
+    "lbm_sparse_set_stream": (ctypes.c_int, [_P, _P]),
+    "lbm_sparse_timestep_even_force": (ctypes.c_int, [_P, _P, _I64, _I64]),
+    "lbm_sparse_timestep_odd_force": (ctypes.c_int, [_P, _P, _I64, _I64]),
+    "lbm_sparse_timestep_force": (ctypes.c_int, [_P, _P, _P, _I64, _I64]),
     "lbm_reduce_conserved_noalloc": (ctypes.c_int, [ctypes.c_int] * 5 + [_I64, _P, _P, _P, ctypes.c_int, _P, _P]),
 }
 

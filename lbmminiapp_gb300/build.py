@@ -29,6 +29,7 @@ SOURCES = [
     "lbm_step_q27_f64.cu",
     "lbm_step_q27_low.cu",
     "lbm_noalloc.cu",
+    "lbm_sparse.cu",
     "lbm_adjoint.cu",
 ]
 

@@ -127,50 +127,13 @@ KParams make_params(const lbm_handle* h, int64_t start, int64_t end, Launch& L)
    const int64_t nxy = (int64_t)c.nx * c.ny;
    const int64_t z0 = start / nxy, z1 = (end - 1) / nxy + 1;
    p.z0 = (int)z0;
-   p.omega = c.omega;
-   p.om1 = 1.0 - c.omega;
-   p.om2 = 1.0 - 0.5 * c.omega;
-   p.omegaf = (float)p.omega;
-   p.om1f = (float)p.om1;
-   p.om2f = (float)p.om2;
-   for (int d = 0; d < 3; d++) {
-      p.F[d] = c.force[d];
-      p.Ff[d] = (float)c.force[d];
-   }
-   p.compat = (c.unroll && h->Q == 19 && c.prop_pattern == LBM_PATTERN_AA) ? 1 : 0;
+   set_collision_constants(p, h->Q, c.omega, c.force,
+                           (c.unroll && h->Q == 19 && c.prop_pattern == LBM_PATTERN_AA) ? 1 : 0);
    p.links = h->links;
    p.force_field = h->force_field;
    p.force_field_f = h->force_field_f;
    p.porosity = h->porosity;
    p.porosity_f = h->porosity_f;
-   auto split = [](double d, float* out) {
-      const float hi = (float)d;
-      out[0] = hi;
-      out[1] = (float)(d - (double)hi);
-   };
-   split(p.om1, p.x_om1);
-   split(p.omega, p.x_omega);
-   for (int k = 0; k < 4; k++) {
-      double w;
-      if (h->Q == 19) w = k == 0 ? 1.0 / 3.0 : (k == 1 ? 1.0 / 18.0 : 1.0 / 36.0);
-      else w = k == 0 ? 8.0 / 27.0 : (k == 1 ? 2.0 / 27.0 : (k == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
-      split(c.omega * w, p.x_ow[k]);
-   }
-   for (int d = 0; d < 3; d++) split(c.force[d], p.x_F[d]);
-   for (int s = 0; s < h->Q; s++) {
-      const double cf = 3.0 * (lat_c(h->Q, s, 0) * c.force[0] + lat_c(h->Q, s, 1) * c.force[1] +
-                               lat_c(h->Q, s, 2) * c.force[2]);
-      split(p.om2 * lat_w(h->Q, s) * cf, p.x_Kf[s]);
-   }
-   for (int d = 0; d < 3; d++) split(3.0 * c.force[d], p.x_F3[d]);
-   for (int k = 0; k < 4; k++) {
-      double w;
-      if (h->Q == 19) w = k == 0 ? 1.0 / 3.0 : (k == 1 ? 1.0 / 18.0 : 1.0 / 36.0);
-      else w = k == 0 ? 8.0 / 27.0 : (k == 1 ? 2.0 / 27.0 : (k == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
-      split(p.om2 * w, p.x_om2w[k]);
-   }
-   split(p.om2 / 36.0, p.x_om2w36);
-   p.forced = (c.force[0] != 0.0 || c.force[1] != 0.0 || c.force[2] != 0.0) ? 1 : 0;
    int bx = (int)std::min<int64_t>(256, ((c.nx + 31) / 32) * 32);
    L.block = dim3(bx, 1, 1);
    L.grid = dim3((c.nx + bx - 1) / bx, c.ny, (unsigned)(z1 - z0));

@@ -363,6 +363,45 @@ struct Consts {
 
 }  // namespace x64
 
+// Host: the collision constants of a launch (relaxation rate, uniform force,
+// the Q19 AA Unroll rest-weight switch) in double, float and float-pair form.
+inline void set_collision_constants(KParams& p, int Q, double omega, const double force[3], int compat)
+{
+   p.omega = omega;
+   p.om1 = 1.0 - omega;
+   p.om2 = 1.0 - 0.5 * omega;
+   p.omegaf = (float)p.omega;
+   p.om1f = (float)p.om1;
+   p.om2f = (float)p.om2;
+   for (int d = 0; d < 3; d++) {
+      p.F[d] = force[d];
+      p.Ff[d] = (float)force[d];
+   }
+   p.compat = compat;
+   auto split = [](double d, float* out) {
+      const float hi = (float)d;
+      out[0] = hi;
+      out[1] = (float)(d - (double)hi);
+   };
+   split(p.om1, p.x_om1);
+   split(p.omega, p.x_omega);
+   for (int k = 0; k < 4; k++) {
+      double w;
+      if (Q == 19) w = k == 0 ? 1.0 / 3.0 : (k == 1 ? 1.0 / 18.0 : 1.0 / 36.0);
+      else w = k == 0 ? 8.0 / 27.0 : (k == 1 ? 2.0 / 27.0 : (k == 2 ? 1.0 / 54.0 : 1.0 / 216.0));
+      split(omega * w, p.x_ow[k]);
+      split(p.om2 * w, p.x_om2w[k]);
+   }
+   for (int d = 0; d < 3; d++) split(force[d], p.x_F[d]);
+   for (int s = 0; s < Q; s++) {
+      const double cf = 3.0 * (lat_c(Q, s, 0) * force[0] + lat_c(Q, s, 1) * force[1] + lat_c(Q, s, 2) * force[2]);
+      split(p.om2 * lat_w(Q, s) * cf, p.x_Kf[s]);
+   }
+   for (int d = 0; d < 3; d++) split(3.0 * force[d], p.x_F3[d]);
+   split(p.om2 / 36.0, p.x_om2w36);
+   p.forced = (force[0] != 0.0 || force[1] != 0.0 || force[2] != 0.0) ? 1 : 0;
+}
+
 // Representative s < opp(s) of the p-th opposite pair (direction order of
 // the reference: pairs are (0,1), (2,3), ... with the rest direction last).
 __host__ __device__ constexpr int pair_dir(int Q, int p)

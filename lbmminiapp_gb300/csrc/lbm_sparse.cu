@@ -1,0 +1,253 @@
+// Compact fluid-only layout: the reference's own population buffers and
+// adjacency list.
+//
+// The reference stores populations only for fluid points, direction s of
+// fluid point i at dstrb[nFluid*s + i], and streams through an int32
+// adjacency list built by GeometryAAAB::setupAdjacency
+// (src/geometries/GeometryAAAB.cpp:18-124): adjacency[nFluid*s + i] is the
+// element index of slot s at the neighbour x - c_s (AA, AB pull) or x + c_s
+// (AB push), or of the own slot opp(s) when that neighbour is a wall.  These
+// kernels run the same steps on those buffers, so a caller that already
+// holds the reference's geometry can keep its layout and ordering:
+//
+//   AA even  (KernelAA_SOA_Base.cpp:173-254): d_s = dstrb[nF*opp(s) + i], out_s -> dstrb[nF*s + i]
+//   AA odd   (KernelAA_SOA_Base.cpp:257-342): loc_s = adj[nF*s + i], d_s = dstrb[loc_s],
+//            out_s -> dstrb[loc_opp(s)]
+//   AB push  (KernelAB_SOA_Base.cpp:111-186): d_s = src[nF*s + i], out_s -> tgt[adj[nF*s + i]]
+//   AB pull  (KernelAB_SOA_Pull.cpp:113-194): d_s = src[adj[nF*s + i]], out_s -> tgt[nF*s + i]
+//
+// One thread per fluid index; FP64 storage with the exact reference-order
+// arithmetic or F64X.  The layout suits media with few fluid cells, where
+// a dense grid would hold and scan every solid cell; the price is the
+// 4*Q bytes of adjacency each AA odd / AB update reads.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm_gb300.h"
+#include "lbm_f64x.cuh"
+
+using namespace lbm;
+
+struct lbm_sparse_handle {
+   int Q = 19;
+   int pattern = LBM_PATTERN_AA;
+   int pull = 0;
+   int arith = AR_F64X;
+   int device = 0;
+   int64_t nfluid = 0;
+   int32_t* adj = nullptr;   // device [Q][nfluid]
+   KParams params;
+   cudaStream_t stream = nullptr;
+   std::string err;
+};
+
+namespace {
+
+constexpr int kSparseThreads = 256;
+
+lbm_status sfail(lbm_sparse_handle* h, lbm_status s, const char* fmt, ...)
+{
+   if (h) {
+      char buf[512];
+      va_list ap;
+      va_start(ap, fmt);
+      vsnprintf(buf, sizeof(buf), fmt, ap);
+      va_end(ap);
+      h->err = buf;
+   }
+   return s;
+}
+
+template <int Q, int AR, int KIND>
+__global__ void __launch_bounds__(kSparseThreads) sparse_step_kernel(const KParams p, const int32_t* __restrict__ adj,
+                                                                     int64_t nfluid, int64_t start, int64_t count,
+                                                                     const double* src, double* dst)
+{
+   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+   if (k >= count) return;
+   const int64_t i = start + k;
+   // Element indices fit 32 bits: the reference's int32 adjacency requires
+   // Q * nFluid < 2^31.
+   const uint32_t nf = (uint32_t)nfluid, ii = (uint32_t)i;
+   uint32_t loc[Q];
+   double d[Q];
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      if (KIND == K_AA_EVEN) loc[s] = nf * (uint32_t)lat_opp(Q, s) + ii;
+      else if (KIND == K_AB_PUSH) loc[s] = nf * (uint32_t)s + ii;
+      else loc[s] = (uint32_t)adj[(size_t)nf * s + ii];
+      d[s] = src[loc[s]];
+   }
+   double o[Q];
+   if constexpr (AR == AR_F64) {
+      collide_f64<Q>(d, o, p.F[0], p.F[1], p.F[2], 0.0, p);
+   } else {
+      uint64_t bits[Q];
+#pragma unroll
+      for (int s = 0; s < Q; s++) bits[s] = x64::double_bits(d[s]);
+      collide_f64x<Q>(bits, p);
+#pragma unroll
+      for (int s = 0; s < Q; s++) o[s] = x64::as_double(bits[s]);
+   }
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      uint32_t w;
+      if (KIND == K_AA_EVEN || KIND == K_AB_PULL) w = nf * (uint32_t)s + ii;
+      else if (KIND == K_AA_ODD) w = loc[lat_opp(Q, s)];
+      else w = (uint32_t)adj[(size_t)nf * s + ii];
+      dst[w] = o[s];
+   }
+}
+
+template <int Q, int AR>
+cudaError_t launch_sparse_q(int kind, const KParams& p, const int32_t* adj, int64_t nfluid, int64_t start,
+                            int64_t count, const double* src, double* dst, cudaStream_t stream)
+{
+   const unsigned grid = (unsigned)((count + kSparseThreads - 1) / kSparseThreads);
+   switch (kind) {
+      case K_AA_EVEN:
+         sparse_step_kernel<Q, AR, K_AA_EVEN><<<grid, kSparseThreads, 0, stream>>>(p, adj, nfluid, start, count, src, dst);
+         break;
+      case K_AA_ODD:
+         sparse_step_kernel<Q, AR, K_AA_ODD><<<grid, kSparseThreads, 0, stream>>>(p, adj, nfluid, start, count, src, dst);
+         break;
+      case K_AB_PUSH:
+         sparse_step_kernel<Q, AR, K_AB_PUSH><<<grid, kSparseThreads, 0, stream>>>(p, adj, nfluid, start, count, src, dst);
+         break;
+      default:
+         sparse_step_kernel<Q, AR, K_AB_PULL><<<grid, kSparseThreads, 0, stream>>>(p, adj, nfluid, start, count, src, dst);
+         break;
+   }
+   return cudaGetLastError();
+}
+
+lbm_status sparse_launch(lbm_sparse_handle* h, int kind, const void* src, void* dst, int64_t start, int64_t count)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (!src || !dst) return sfail(h, LBM_ERR_INVALID_ARGUMENT, "null population buffer");
+   if (start < 0 || count < 0 || start + count > h->nfluid)
+      return sfail(h, LBM_ERR_INVALID_ARGUMENT, "range [%lld, %lld) outside [0, %lld)", (long long)start,
+                   (long long)(start + count), (long long)h->nfluid);
+   if (count == 0) return LBM_OK;
+   int cur = -1;
+   if (cudaGetDevice(&cur) != cudaSuccess || cur != h->device) {
+      cudaError_t e = cudaSetDevice(h->device);
+      if (e != cudaSuccess) return sfail(h, LBM_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
+   }
+   const double* s = static_cast<const double*>(src);
+   double* d = static_cast<double*>(dst);
+   cudaError_t e;
+   if (h->Q == 19)
+      e = h->arith == AR_F64 ? launch_sparse_q<19, AR_F64>(kind, h->params, h->adj, h->nfluid, start, count, s, d, h->stream)
+                             : launch_sparse_q<19, AR_F64X>(kind, h->params, h->adj, h->nfluid, start, count, s, d, h->stream);
+   else
+      e = h->arith == AR_F64 ? launch_sparse_q<27, AR_F64>(kind, h->params, h->adj, h->nfluid, start, count, s, d, h->stream)
+                             : launch_sparse_q<27, AR_F64X>(kind, h->params, h->adj, h->nfluid, start, count, s, d, h->stream);
+   if (e != cudaSuccess) return sfail(h, LBM_ERR_CUDA, "sparse step launch: %s", cudaGetErrorString(e));
+   return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_sparse_create(const lbm_config* cfg, int64_t nfluid, const int32_t* adjacency, lbm_sparse_handle** out)
+{
+   if (!out) return LBM_ERR_INVALID_ARGUMENT;
+   *out = nullptr;
+   if (!cfg || !adjacency) return LBM_ERR_INVALID_ARGUMENT;
+   if (cfg->lattice != 19 && cfg->lattice != 27) return LBM_ERR_INVALID_ARGUMENT;
+   if (cfg->prop_pattern != LBM_PATTERN_AA && cfg->prop_pattern != LBM_PATTERN_AB) return LBM_ERR_INVALID_ARGUMENT;
+   if (cfg->storage != LBM_STORE_F64) return LBM_ERR_UNSUPPORTED;
+   if (cfg->arithmetic != LBM_ARITH_AUTO && cfg->arithmetic != LBM_ARITH_F64 && cfg->arithmetic != LBM_ARITH_F64X)
+      return LBM_ERR_UNSUPPORTED;
+   const int Q = cfg->lattice;
+   // The reference's int32 slot indices limit Q * nFluid to 2^31 - 1.
+   if (nfluid <= 0 || (int64_t)Q * nfluid > 0x7FFFFFFFll) return LBM_ERR_INVALID_ARGUMENT;
+   const int64_t n = (int64_t)Q * nfluid;
+   for (int64_t k = 0; k < n; k++)
+      if (adjacency[k] < 0 || (int64_t)adjacency[k] >= n) return LBM_ERR_INVALID_ARGUMENT;
+   lbm_sparse_handle* h = new (std::nothrow) lbm_sparse_handle();
+   if (!h) return LBM_ERR_OUT_OF_MEMORY;
+   h->Q = Q;
+   h->pattern = cfg->prop_pattern;
+   h->pull = cfg->pull ? 1 : 0;
+   h->arith = cfg->arithmetic == LBM_ARITH_F64 ? AR_F64 : AR_F64X;
+   h->device = cfg->device;
+   h->nfluid = nfluid;
+   std::memset(&h->params, 0, sizeof(h->params));
+   set_collision_constants(h->params, Q, cfg->omega, cfg->force,
+                           (cfg->unroll && Q == 19 && cfg->prop_pattern == LBM_PATTERN_AA) ? 1 : 0);
+   cudaError_t e = cudaSetDevice(cfg->device);
+   const size_t bytes = (size_t)n * sizeof(int32_t);
+   if (e == cudaSuccess && cfg->max_device_bytes && bytes > cfg->max_device_bytes) {
+      delete h;
+      return LBM_ERR_OUT_OF_MEMORY;
+   }
+   if (e == cudaSuccess) e = cudaMalloc(&h->adj, bytes);
+   if (e == cudaSuccess) e = cudaMemcpy(h->adj, adjacency, bytes, cudaMemcpyHostToDevice);
+   if (e != cudaSuccess) {
+      cudaGetLastError();
+      if (h->adj) cudaFree(h->adj);
+      const bool oom = e == cudaErrorMemoryAllocation;
+      delete h;
+      return oom ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA;
+   }
+   *out = h;
+   return LBM_OK;
+}
+
+void lbm_sparse_destroy(lbm_sparse_handle* h)
+{
+   if (!h) return;
+   if (h->adj) {
+      cudaSetDevice(h->device);
+      cudaFree(h->adj);
+   }
+   delete h;
+}
+
+const char* lbm_sparse_last_error(const lbm_sparse_handle* h)
+{
+   if (!h) return "null handle";
+   return h->err.c_str();
+}
+
+lbm_status lbm_sparse_set_stream(lbm_sparse_handle* h, void* stream)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   h->stream = static_cast<cudaStream_t>(stream);
+   return LBM_OK;
+}
+
+lbm_status lbm_sparse_timestep_even_force(lbm_sparse_handle* h, double* dstrb, int64_t start, int64_t count)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->pattern != LBM_PATTERN_AA) return sfail(h, LBM_ERR_STATE, "even/odd steps need an AA handle");
+   return sparse_launch(h, K_AA_EVEN, dstrb, dstrb, start, count);
+}
+
+lbm_status lbm_sparse_timestep_odd_force(lbm_sparse_handle* h, double* dstrb, int64_t start, int64_t count)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->pattern != LBM_PATTERN_AA) return sfail(h, LBM_ERR_STATE, "even/odd steps need an AA handle");
+   return sparse_launch(h, K_AA_ODD, dstrb, dstrb, start, count);
+}
+
+lbm_status lbm_sparse_timestep_force(lbm_sparse_handle* h, const double* src, double* tgt, int64_t start,
+                                     int64_t count)
+{
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->pattern != LBM_PATTERN_AB) return sfail(h, LBM_ERR_STATE, "timestep_force needs an AB handle");
+   if (src == tgt) return sfail(h, LBM_ERR_INVALID_ARGUMENT, "AB needs two distinct buffers");
+   return sparse_launch(h, h->pull ? K_AB_PULL : K_AB_PUSH, src, tgt, start, count);
+}
+
+}  // extern "C"

@@ -63,6 +63,7 @@ def lib(Q: int) -> ctypes.CDLL:
         L.ref_box_run.restype = ctypes.c_int
         L.ref_app_prepare.argtypes = [ctypes.c_char_p, ctypes.c_double, ctypes.c_double, P, P, P, P]
         L.ref_app_execute.argtypes = [P, P, P, P]
+        L.ref_app_execute_compact.argtypes = [P, P, P, P, P]
         _libs[Q] = L
     return _libs[Q]
 
@@ -106,3 +107,30 @@ def app_run(Q, input_file, omega=1.0, gx=1e-6):
     L.ref_app_execute(_ptr(rho), _ptr(u), _ptr(f), ctypes.byref(sec))
     return dict(dims=(nx, ny, nz), nfluid=nf.value, steps=steps.value, prop_pattern=pp.value,
                 rho=rho, u=u, f_raw=f, seconds=sec.value)
+
+
+def app_run_compact(Q, input_file, omega=1.0, gx=1e-6):
+    """The reference's single-rank flow on one of its input files, returning
+    its own compact buffers: dict(dims, nfluid, steps, prop_pattern,
+    adjacency [Q, nfluid] int32 (GeometryAAAB::setupAdjacency), fluid_pts
+    [nfluid, 3] (i, j, k) in the reference's sorted order, raw_init and
+    raw_final [Q, nfluid] (population buffer before and after the run),
+    seconds)."""
+    L = lib(Q)
+    dims = (ctypes.c_int * 3)()
+    nf = ctypes.c_longlong()
+    steps = ctypes.c_int()
+    pp = ctypes.c_int()
+    L.ref_app_prepare(str(input_file).encode(), float(omega), float(gx), dims, ctypes.byref(nf),
+                      ctypes.byref(steps), ctypes.byref(pp))
+    n = nf.value
+    adj = np.empty((Q, n), np.int32)
+    pts = np.empty((n, 3), np.int32)
+    f0 = np.empty((Q, n))
+    f1 = np.empty((Q, n))
+    sec = ctypes.c_double()
+    rc = L.ref_app_execute_compact(_ptr(f0), _ptr(f1), _ptr(adj), _ptr(pts), ctypes.byref(sec))
+    if rc:
+        raise RuntimeError(f"ref_app_execute_compact failed with code {rc}")
+    return dict(dims=(dims[0], dims[1], dims[2]), nfluid=n, steps=steps.value, prop_pattern=pp.value,
+                adjacency=adj, fluid_pts=pts, raw_init=f0, raw_final=f1, seconds=sec.value)

@@ -347,4 +347,46 @@ int ref_app_execute(double* rho, double* u, double* f_raw, double* seconds)
    return 0;
 }
 
+/*
+ * Part 2, compact form: the same run, returning the reference's own buffers
+ * in its own layout instead of dense arrays -- the raw population buffer
+ * before the run (raw_init, the rest state PropagationAA/AB::initialize
+ * wrote) and after it (raw_final), both [Q][nFluid]; the adjacency list of
+ * GeometryAAAB::setupAdjacency, [Q][nFluid]; the fluid points in the
+ * reference's sorted order, [nFluid][3] as (i, j, k).
+ */
+int ref_app_execute_compact(double* raw_init, double* raw_final, int* adjacency, int* fluid_pts,
+                            double* seconds)
+{
+   if (!g_app.geometry) return 1;
+   Geometry& g = *g_app.geometry;
+   const int Q = _LATTICESIZE_;
+   const int nFluid = g.getNumFluidPts();
+   for (size_t k = 0; k < (size_t)Q * nFluid; k++) adjacency[k] = g.adjacency_[k];
+   for (int f = 0; f < nFluid; f++)
+      for (int d = 0; d < 3; d++) fluid_pts[3 * f + d] = g.fluidPts_[f][d];
+   Pdf* raw = nullptr;
+   auto t0 = std::chrono::steady_clock::now();
+   if (g_app.parameters->getPropPattern() == 1) {
+      g_app.aa = new ExposedAA(*g_app.lattice, g, *g_app.comm, *g_app.parameters);
+      g_app.aa->setup();
+      g_app.aa->initialize();
+      for (size_t k = 0; k < (size_t)Q * nFluid; k++) raw_init[k] = g_app.aa->raw()[k];
+      g_app.aa->run();
+      raw = g_app.aa->raw();
+   } else {
+      g_app.ab = new ExposedAB(*g_app.lattice, g, *g_app.comm, *g_app.parameters);
+      g_app.ab->setup();
+      g_app.ab->initialize();
+      for (size_t k = 0; k < (size_t)Q * nFluid; k++) raw_init[k] = g_app.ab->raw()[k];
+      g_app.ab->run();
+      raw = g_app.ab->raw();
+   }
+   auto t1 = std::chrono::steady_clock::now();
+   if (seconds) *seconds = std::chrono::duration<double>(t1 - t0).count();
+   for (size_t k = 0; k < (size_t)Q * nFluid; k++) raw_final[k] = raw[k];
+   app_release();
+   return 0;
+}
+
 }  // extern "C"

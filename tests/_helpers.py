@@ -11,12 +11,17 @@ PATTERN_NAMES = {0: "aa", 1: "ab_push", 2: "ab_pull"}
 
 def golden_cases():
     """Box / channel cases (reference kernels on a harness geometry)."""
-    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("cylinder_"))
+    return sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith(("cylinder_", "sparse_")))
 
 
 def cylinder_cases():
     """The reference's whole app flow on its cylinder (centre plane kept)."""
     return sorted(p.stem for p in GOLDEN.glob("cylinder_*.npz"))
+
+
+def sparse_cases():
+    """The reference's own compact buffers and adjacency (cylinder, size 0.25)."""
+    return sorted(p.stem for p in GOLDEN.glob("sparse_*.npz"))
 
 
 def load_golden(name):

@@ -77,6 +77,34 @@ def make_cylinder(tmpdir):
         print(f"{name}: nfluid {out['nfluid']}")
 
 
+# Compact-layout cases: the reference's own sorted fluid list, adjacency
+# (GeometryAAAB::setupAdjacency) and final raw population buffer of a size-0.25
+# cylinder (21 x 7 x 7, 672 fluid points) run through its app flow with the
+# Base kernels (unroll 0).  The initial buffer is the rest state: every slot s
+# holds w_s (checked here, so the tests rebuild it instead of storing it).
+SPARSE_CASES = {
+    "sparse_q19_aa_cylinder": dict(Q=19, propPattern=1, pull=0),
+    "sparse_q19_ab_push_cylinder": dict(Q=19, propPattern=0, pull=0),
+    "sparse_q19_ab_pull_cylinder": dict(Q=19, propPattern=0, pull=1),
+    "sparse_q27_aa_cylinder": dict(Q=27, propPattern=1, pull=0),
+}
+SPARSE_SIZE, SPARSE_STEPS, SPARSE_OMEGA, SPARSE_GX = 0.25, 12, 1.0 / 0.7, 1e-4
+
+
+def make_sparse(tmpdir):
+    for name, keys in SPARSE_CASES.items():
+        Q = keys["Q"]
+        inp = cylinder_input(Path(tmpdir) / f"{name}.txt", keys["propPattern"], keys["pull"], 0,
+                             steps=SPARSE_STEPS, size=SPARSE_SIZE)
+        out = ref.app_run_compact(Q, inp, omega=SPARSE_OMEGA, gx=SPARSE_GX)
+        _, _, w = core.stencil(Q)
+        assert np.array_equal(out["raw_init"], np.repeat(w[:, None], out["nfluid"], axis=1))
+        np.savez_compressed(HERE / f"{name}.npz", Q=Q, prop_pattern=keys["propPattern"], pull=keys["pull"],
+                            dims=np.array(out["dims"]), steps=out["steps"], omega=SPARSE_OMEGA, gx=SPARSE_GX,
+                            fluid_pts=out["fluid_pts"], adjacency=out["adjacency"], raw_final=out["raw_final"])
+        print(f"{name}: nfluid {out['nfluid']}")
+
+
 # The reference's VTK output (Propagation::writeVTK, src/propagation/
 # Propagation.cpp:36-161) of a size-1 AA Unroll cylinder run: the header and
 # the rho and velocity sections as the reference printed them (its "id"
@@ -121,6 +149,8 @@ def main():
         make_cylinder(tmp)
     with tempfile.TemporaryDirectory() as tmp:
         make_vtk(tmp)
+    with tempfile.TemporaryDirectory() as tmp:
+        make_sparse(tmp)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,135 @@
+"""Compact fluid-only layout on the GPU (lbm_sparse_*): the reference's own
+buffers, fluid order and adjacency list for its cylinder, stepped by the CUDA
+kernels and compared with the reference's final raw buffer
+(tests/golden/sparse_*.npz, made by tests/golden/make_golden.py from the
+reference's app flow with the Base kernels).  Exact FP64 arithmetic must be
+bit-identical; F64X within 1e-10 relative."""
+import numpy as np
+import pytest
+
+from _helpers import load_golden, rel_err, sparse_cases
+from lbmminiapp_gb300 import cylinder, sparse
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+PATTERNS = {(1, 0): "aa", (0, 0): "ab_push", (0, 1): "ab_pull"}
+
+
+def weights(Q):
+    if Q == 19:
+        table = {0: 1.0 / 3.0, 1: 1.0 / 18.0, 2: 1.0 / 36.0}
+    else:
+        table = {0: 8.0 / 27.0, 1: 2.0 / 27.0, 2: 1.0 / 54.0, 3: 1.0 / 216.0}
+    c = sparse.velocities(Q)
+    return np.array([table[int(k)] for k in (c * c).sum(axis=1)])
+
+
+def run_case(g, arithmetic, adjacency=None, chunks=1):
+    """Rest start (every slot s holds w_s, as PropagationAA/AB::initialize
+    writes it), g['steps'] steps; returns the final raw buffer [Q, nfluid]."""
+    Q = int(g["Q"])
+    adj = g["adjacency"] if adjacency is None else adjacency
+    n = adj.shape[1]
+    pattern = PATTERNS[(int(g["prop_pattern"]), int(g["pull"]))]
+    f0 = np.repeat(weights(Q)[:, None], n, axis=1)
+    bufs = [torch.tensor(f0, dtype=torch.float64, device="cuda") for _ in range(1 if pattern == "aa" else 2)]
+    with sparse.SparseKernels(adj, lattice=Q, pattern=pattern, omega=float(g["omega"]),
+                              force=(float(g["gx"]), 0.0, 0.0), arithmetic=arithmetic) as k:
+        if chunks == 1:
+            out = k.run(bufs, int(g["steps"]))
+        else:
+            # border/bulk-style range calls (PropagationAA.cpp:173-174)
+            edges = np.linspace(0, n, chunks + 1).astype(int)
+            src = bufs[0]
+            tgt = bufs[1] if len(bufs) > 1 else None
+            for t in range(int(g["steps"])):
+                for a, b in zip(edges[:-1], edges[1:]):
+                    if pattern == "aa":
+                        (k.timestep_even_force if t % 2 == 0 else k.timestep_odd_force)(src, int(a), int(b - a))
+                    else:
+                        k.timestep_force(src, tgt, int(a), int(b - a))
+                if tgt is not None:
+                    src, tgt = tgt, src
+            out = src
+        torch.cuda.synchronize()
+        return out.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", sparse_cases())
+def test_exact_arithmetic_is_bit_identical_to_reference(gpu, name):
+    g = load_golden(name)
+    out = run_case(g, "f64")
+    assert np.array_equal(out, g["raw_final"]), rel_err(out, g["raw_final"])
+
+
+@pytest.mark.parametrize("name", sparse_cases())
+def test_f64x_within_1e10_of_reference(gpu, name):
+    g = load_golden(name)
+    out = run_case(g, "f64x")
+    assert rel_err(out, g["raw_final"]) <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["sparse_q19_aa_cylinder", "sparse_q19_ab_pull_cylinder"])
+def test_range_calls_compose(gpu, name):
+    g = load_golden(name)
+    assert np.array_equal(run_case(g, "f64", chunks=3), g["raw_final"])
+
+
+@pytest.mark.parametrize("name", ["sparse_q19_aa_cylinder", "sparse_q19_ab_push_cylinder"])
+def test_any_fluid_order(gpu, name):
+    """The same geometry in a shuffled fluid order gives the shuffled result."""
+    g = load_golden(name)
+    adj = g["adjacency"].astype(np.int64)
+    Q, n = adj.shape
+    perm = np.random.default_rng(5).permutation(n)
+    inv = np.empty(n, np.int64)
+    inv[perm] = np.arange(n)
+    s_part, j_part = np.divmod(adj[:, perm], n)
+    adj_p = (s_part * n + inv[j_part]).astype(np.int32)
+    out = run_case(g, "f64", adjacency=adj_p)
+    assert np.array_equal(out, g["raw_final"][:, perm])
+
+
+@pytest.mark.parametrize("pattern", ["aa", "ab_push", "ab_pull"])
+def test_matches_dense_layout_on_larger_cylinder(gpu, pattern):
+    """build_adjacency + the compact kernels against the dense-layout path
+    (link words) on a size-1 cylinder, exact FP64 arithmetic: the same
+    populations bit for bit."""
+    import lbmminiapp_gb300 as lbm
+    dims, solid = cylinder(1.0)
+    nx, ny, nz = dims
+    cells, adj = sparse.build_adjacency(solid, (1, 0, 0), pattern, 19)
+    omega, gx, steps = 1.0 / 0.6, 1e-5, 9
+    with lbm.Simulation(nx, ny, nz, lattice=19, pattern=pattern, omega=omega, force=(gx, 0, 0),
+                        periodic=(1, 0, 0), arithmetic="f64") as sim:
+        sim.set_solid(solid)
+        sim.init_equilibrium(None, None)
+        sim.step(steps)
+        dense = sim.get_populations("raw").reshape(19, -1)[:, cells]
+    g = dict(Q=19, prop_pattern=1 if pattern == "aa" else 0, pull=int(pattern == "ab_pull"), omega=omega,
+             gx=gx, steps=steps, adjacency=adj)
+    out = run_case(g, "f64")
+    assert np.array_equal(out, dense)
+
+
+def test_errors_are_reported(gpu):
+    g = load_golden("sparse_q19_aa_cylinder")
+    n = g["adjacency"].shape[1]
+    buf = torch.zeros((19, n), dtype=torch.float64, device="cuda")
+    with sparse.SparseKernels(g["adjacency"], lattice=19, pattern="aa") as k:
+        with pytest.raises(lbm_error()) as e:
+            k.timestep_force(buf, buf)
+        assert e.value.status == 6
+        with pytest.raises(lbm_error()) as e:
+            k.timestep_even_force(buf, 0, n + 1)
+        assert e.value.status == 1
+    bad = g["adjacency"].copy()
+    bad[3, 5] = 19 * n
+    with pytest.raises(lbm_error()):
+        sparse.SparseKernels(bad, lattice=19, pattern="aa")
+
+
+def lbm_error():
+    from lbmminiapp_gb300 import LBMError
+    return LBMError
