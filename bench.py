@@ -10,8 +10,8 @@ is one lattice time step over the whole box (one kernel launch); the state is
 * value      MLUPS with the state resident in HBM, CUDA events on the launch
              stream, max over ranks (independent replicas when --gpus > 1);
 * e2e        the same metric through the C ABI from pinned host memory: the
-             initial velocity field is copied in, 100 steps run and rho/u are
-             copied back, all inside the timed region;
+             whole workload -- the initial velocity field copied in, its 1000
+             steps, rho/u copied back -- inside the timed region;
 * roofline   HBM bound: algorithmic bytes 2*Q*8 = 304 B per fluid-cell update
              over the measured copy bandwidth (MEASURED_PEAKS.json);
 * cpu_baseline  the oracle port (C restatement of the reference's CPU kernels,
@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--n", type=int, default=512, help="box edge (cells)")
     ap.add_argument("--no-variants", action="store_true", help="skip the other storage formats")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=1000,
+                    help="lattice steps of the end-to-end round trip (the workload's 1000 steps)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--storage", default="f64", choices=["f64", "f32", "bf16", "f16"],
                     help="population storage of the timed run (headline: f64)")
@@ -368,17 +370,17 @@ def main():
     # end to end through the C ABI, pinned host buffers
     e2e = None
     if not args.no_e2e:
-        steps_e2e = 100
+        steps_e2e = args.e2e_steps
         u_host = torch.empty((3, n, n, n), dtype=torch.float64, pin_memory=True)
         u_host.numpy()[...] = u
         rho_out = torch.empty((n, n, n), dtype=torch.float64, pin_memory=True)
         u_out = torch.empty((3, n, n, n), dtype=torch.float64, pin_memory=True)
         times = []
-        for rep in range(2):
+        for nsteps in (10, steps_e2e):   # a short warm-up round trip, then the timed one
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             sim.init_equilibrium(None, u_host.numpy())
-            sim.step(steps_e2e)
+            sim.step(nsteps)
             sim.macros(out=(rho_out.numpy(), u_out.numpy()))
             times.append(time.perf_counter() - t0)
         launches_e2e = steps_e2e + 2

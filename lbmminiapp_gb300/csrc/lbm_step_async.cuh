@@ -67,43 +67,43 @@ __device__ __forceinline__ void cp_async8(uint32_t smem, const void* g)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
-// Addresses: plane base (slot * plane, the same for every tile) plus a
-// 32-bit cell index (fewer than 2^31 cells; the periodic wrap keeps
-// neighbour indices inside the box).
+// Base pointer of every direction plane of the source and target buffers,
+// passed by value so each sits in the kernel's parameter bank: an access is
+// then one wide multiply-add of a 32-bit cell index (fewer than 2^31 cells;
+// the periodic wrap keeps neighbour indices inside the box) onto a
+// parameter-bank pointer.
+struct PlanePtrs {
+   const unsigned long long* src[27];
+   unsigned long long* dst[27];
+};
+
 template <int Q, int KIND>
-__device__ __forceinline__ void async_issue(const unsigned long long* src, int64_t plane, const CellIndex& ci,
-                                            int lane, uint32_t sbuf)
+__device__ __forceinline__ void async_issue(const PlanePtrs& pp, const CellIndex& ci, int lane, uint32_t sbuf)
 {
    const uint32_t c = (uint32_t)ci.c;
 #pragma unroll
    for (int s = 0; s < Q; s++) {
       const Access a = read_access<Q, KIND, false>(ci, 0u, s);
-      const unsigned long long* plane_base = src + a.slot * plane;
-      cp_async8(sbuf + (uint32_t)(s * 32 + lane) * 8u, plane_base + (c + (uint32_t)a.off));
+      cp_async8(sbuf + (uint32_t)(s * 32 + lane) * 8u, pp.src[a.slot] + (c + (uint32_t)a.off));
    }
 }
 
 template <int Q, int KIND>
 __global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KParams p, const AsyncGeom ag,
-                                                                      const unsigned long long* src,
-                                                                      unsigned long long* dst)
+                                                                      const PlanePtrs pp)
 {
    extern __shared__ __align__(16) unsigned long long async_smem[];
-   constexpr bool kInPlace = KIND == K_AA_EVEN || KIND == K_AA_ODD;
-   // AA runs in place on one buffer (the caller passes src == dst).
-   unsigned long long* out = kInPlace ? const_cast<unsigned long long*>(src) : dst;
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
    const uint32_t nw = gridDim.x * kAsyncWarps;
    uint32_t t = blockIdx.x * kAsyncWarps + warp;
    if (t >= ag.ntiles) return;
-   const int64_t plane = p.plane;
    unsigned long long* mine = async_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 8;
    CellIndex cur;
    tile_cell(p, ag, t, lane, cur);
-   async_issue<Q, KIND>(src, plane, cur, lane, sbase);
+   async_issue<Q, KIND>(pp, cur, lane, sbase);
    cp_async_commit();
    int stage = 0;
    for (;;) {
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KPar
       CellIndex nxt = cur;
       if (next < ag.ntiles) {
          tile_cell(p, ag, next, lane, nxt);
-         async_issue<Q, KIND>(src, plane, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
+         async_issue<Q, KIND>(pp, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
       }
       cp_async_commit();
       cp_async_wait_prev();
@@ -124,8 +124,7 @@ __global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KPar
 #pragma unroll
       for (int s = 0; s < Q; s++) {
          const Access a = write_access<Q, KIND, false>(cur, 0u, s);
-         unsigned long long* plane_base = out + a.slot * plane;
-         plane_base[c + (uint32_t)a.off] = bits[s];
+         pp.dst[a.slot][c + (uint32_t)a.off] = bits[s];
       }
       if (next >= ag.ntiles) break;
       t = next;
@@ -169,8 +168,13 @@ cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src,
    }
    const uint32_t need = (ag.ntiles + kAsyncWarps - 1) / kAsyncWarps;
    const unsigned grid = (unsigned)(need < (uint32_t)grid_of_device[dev] ? need : (uint32_t)grid_of_device[dev]);
-   kern<<<grid, kAsyncWarps * 32, smem, stream>>>(p, ag, static_cast<const unsigned long long*>(src),
-                                                  static_cast<unsigned long long*>(dst));
+   PlanePtrs pp;
+   for (int s = 0; s < 27; s++) {
+      const int k = s < Q ? s : 0;
+      pp.src[s] = static_cast<const unsigned long long*>(src) + (int64_t)k * p.plane;
+      pp.dst[s] = static_cast<unsigned long long*>(dst) + (int64_t)k * p.plane;
+   }
+   kern<<<grid, kAsyncWarps * 32, smem, stream>>>(p, ag, pp);
    return cudaGetLastError();
 }
 
