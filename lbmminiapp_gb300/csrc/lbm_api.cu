@@ -35,7 +35,11 @@ struct lbm_handle {
    float* force_field_f = nullptr;
    double* porosity = nullptr;
    float* porosity_f = nullptr;
-   double* staging = nullptr;      // one dense double plane
+   double* staging = nullptr;      // one dense double plane (at least kMinStaging doubles)
+   size_t staging_elems = 0;
+   cudaStream_t copy_stream = nullptr;   // host <-> staging copies of the chunked transfers
+   cudaEvent_t chunk_ready[2] = {nullptr, nullptr};
+   cudaEvent_t chunk_free[2] = {nullptr, nullptr};
    double* partials = nullptr;     // reduction scratch: kReduceBlocks * 4 doubles
    double* reduce_out = nullptr;   // 4 doubles
    cudaStream_t stream = nullptr;
@@ -45,6 +49,7 @@ struct lbm_handle {
 namespace {
 
 constexpr int kReduceBlocks = 152 * 8;
+constexpr size_t kMinStaging = 1 << 16;   // doubles
 
 lbm_status fail(lbm_handle* h, lbm_status s, const char* fmt, ...)
 {
@@ -191,10 +196,11 @@ void dispatch_q_st(int Q, int st, A&&... a)
 
 template <int Q, int ST>
 struct InitEq {
-   static void run(const lbm_handle* h, const double* rho, const double* u, int aa)
+   static void run(const lbm_handle* h, int64_t c0, int64_t count, const double* rho, const double* u,
+                   int64_t in_stride, int aa)
    {
-      init_eq_kernel<Q, ST><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(dims_of(h), rho, u, h->buf[0],
-                                                                               h->buf[1], aa);
+      init_eq_kernel<Q, ST><<<blocks_for(count, 256), 256, 0, h->stream>>>(dims_of(h), c0, count, rho, u, in_stride,
+                                                                            h->buf[0], h->buf[1], aa);
    }
 };
 
@@ -218,10 +224,11 @@ struct ExportPlane {
 
 template <int Q, int ST>
 struct Macros {
-   static void run(const lbm_handle* h, const void* buf, int mode, double* rho, double* u)
+   static void run(const lbm_handle* h, int64_t c0, int64_t count, const void* buf, int mode, double* rho,
+                   double* u, int64_t out_stride)
    {
-      macros_kernel<Q, ST><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(dims_of(h), buf, h->links, mode,
-                                                                              rho, u);
+      macros_kernel<Q, ST><<<blocks_for(count, 256), 256, 0, h->stream>>>(dims_of(h), c0, count, buf, h->links,
+                                                                           mode, rho, u, out_stride);
    }
 };
 
@@ -313,6 +320,14 @@ void lbm_destroy(lbm_handle* h)
    cudaFree(h->porosity);
    cudaFree(h->porosity_f);
    cudaFree(h->staging);
+   if (h->copy_stream) {
+      cudaStreamSynchronize(h->copy_stream);
+      cudaStreamDestroy(h->copy_stream);
+   }
+   for (int k = 0; k < 2; k++) {
+      if (h->chunk_ready[k]) cudaEventDestroy(h->chunk_ready[k]);
+      if (h->chunk_free[k]) cudaEventDestroy(h->chunk_free[k]);
+   }
    cudaFree(h->partials);
    cudaFree(h->reduce_out);
    if (prev >= 0) cudaSetDevice(prev);
@@ -372,7 +387,8 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_handle** out)
    }
    if (st == LBM_OK) st = dev_alloc(h, &h->buf[0], h->buffer_bytes);
    if (st == LBM_OK && c.prop_pattern == LBM_PATTERN_AB) st = dev_alloc(h, &h->buf[1], h->buffer_bytes);
-   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->staging, sizeof(double) * (size_t)h->ncell);
+   h->staging_elems = std::max<size_t>((size_t)h->ncell, kMinStaging);
+   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->staging, sizeof(double) * h->staging_elems);
    if (st == LBM_OK) st = dev_alloc(h, (void**)&h->partials, sizeof(double) * 4 * kReduceBlocks);
    if (st == LBM_OK) st = dev_alloc(h, (void**)&h->reduce_out, sizeof(double) * 4);
    if (st == LBM_OK) st = lbm_set_solid(h, nullptr);
@@ -527,34 +543,74 @@ lbm_status lbm_set_porosity(lbm_handle* h, const double* porosity)
    return set_field(h, porosity, 1, &h->porosity, &h->porosity_f);
 }
 
+// Copy stream and events of the chunked host transfers, made on first use.
+static lbm_status ensure_copy_stream(lbm_handle* h)
+{
+   if (h->copy_stream) return LBM_OK;
+   LBM_CUDA(h, cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+   for (int k = 0; k < 2; k++) {
+      LBM_CUDA(h, cudaEventCreateWithFlags(&h->chunk_ready[k], cudaEventDisableTiming));
+      LBM_CUDA(h, cudaEventCreateWithFlags(&h->chunk_free[k], cudaEventDisableTiming));
+   }
+   return LBM_OK;
+}
+
+// Host arrays move through the two halves of the staging plane in chunks of
+// cells: while the kernel works on one half, the copy stream fills (or
+// drains) the other.  ncomp planar components of `chunk` cells fit one half.
+static int64_t chunk_cells(const lbm_handle* h, int ncomp)
+{
+   return (int64_t)((h->staging_elems / 2) / (size_t)ncomp);
+}
+
 lbm_status lbm_init_equilibrium(lbm_handle* h, const double* rho, const double* u)
 {
    if (!h) return LBM_ERR_INVALID_ARGUMENT;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
-   double* drho = nullptr;
-   double* du = nullptr;
-   const size_t n = (size_t)h->ncell;
-   lbm_status st = LBM_OK;
-   if (rho) st = dev_alloc(h, (void**)&drho, sizeof(double) * n);
-   if (st == LBM_OK && u) st = dev_alloc(h, (void**)&du, sizeof(double) * 3 * n);
-   if (st == LBM_OK && rho)
-      LBM_CUDA(h, cudaMemcpyAsync(drho, rho, sizeof(double) * n, cudaMemcpyHostToDevice, h->stream));
-   if (st == LBM_OK && u)
-      LBM_CUDA(h, cudaMemcpyAsync(du, u, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, h->stream));
-   if (st == LBM_OK) {
-      const int aa = h->cfg.prop_pattern == LBM_PATTERN_AA ? 1 : 0;
-      dispatch_q_st<InitEq>(h->Q, h->storage, h, drho, du, aa);
-      cudaError_t e = cudaGetLastError();
-      if (e != cudaSuccess) st = cuda_fail(h, e, "init_eq_kernel");
-      else if ((e = cudaStreamSynchronize(h->stream)) != cudaSuccess) st = cuda_fail(h, e, "init_eq sync");
+   const int aa = h->cfg.prop_pattern == LBM_PATTERN_AA ? 1 : 0;
+   const int64_t n = h->ncell;
+   if (!rho && !u) {
+      dispatch_q_st<InitEq>(h->Q, h->storage, h, (int64_t)0, n, (const double*)nullptr, (const double*)nullptr,
+                            n, aa);
+      LBM_CUDA(h, cudaGetLastError());
+   } else {
+      lbm_status st = ensure_copy_stream(h);
+      if (st != LBM_OK) return st;
+      const int ncomp = (rho ? 1 : 0) + (u ? 3 : 0);
+      const int64_t chunk = chunk_cells(h, ncomp);
+      const size_t half = h->staging_elems / 2;
+      // staging is free once the work already queued on the handle's stream is done
+      for (int b = 0; b < 2; b++) LBM_CUDA(h, cudaEventRecord(h->chunk_free[b], h->stream));
+      for (int64_t c0 = 0, k = 0; c0 < n; c0 += chunk, k++) {
+         const int64_t cnt = std::min<int64_t>(chunk, n - c0);
+         const int b = (int)(k & 1);
+         double* dst = h->staging + b * half;
+         LBM_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->chunk_free[b], 0));
+         double* drho = nullptr;
+         double* du = nullptr;
+         if (rho) {
+            drho = dst;
+            LBM_CUDA(h, cudaMemcpyAsync(drho, rho + c0, sizeof(double) * cnt, cudaMemcpyHostToDevice,
+                                        h->copy_stream));
+         }
+         if (u) {
+            du = dst + (rho ? cnt : 0);
+            for (int d = 0; d < 3; d++)
+               LBM_CUDA(h, cudaMemcpyAsync(du + d * cnt, u + (size_t)d * n + c0, sizeof(double) * cnt,
+                                           cudaMemcpyHostToDevice, h->copy_stream));
+         }
+         LBM_CUDA(h, cudaEventRecord(h->chunk_ready[b], h->copy_stream));
+         LBM_CUDA(h, cudaStreamWaitEvent(h->stream, h->chunk_ready[b], 0));
+         dispatch_q_st<InitEq>(h->Q, h->storage, h, c0, cnt, (const double*)drho, (const double*)du, cnt, aa);
+         LBM_CUDA(h, cudaGetLastError());
+         LBM_CUDA(h, cudaEventRecord(h->chunk_free[b], h->stream));
+      }
    }
-   dev_free(h, drho, sizeof(double) * n);
-   dev_free(h, du, sizeof(double) * 3 * n);
-   if (st == LBM_OK) {
-      h->t = 0;
-      h->cur = 0;
-   }
-   return st;
+   cudaError_t e = cudaStreamSynchronize(h->stream);
+   if (e != cudaSuccess) return cuda_fail(h, e, "init_eq sync");
+   h->t = 0;
+   h->cur = 0;
+   return LBM_OK;
 }
 
 lbm_status lbm_set_populations(lbm_handle* h, const double* f, int layout)
@@ -626,22 +682,31 @@ lbm_status lbm_get_macros(lbm_handle* h, double* rho, double* u)
    // The reference reads AA through the streamed populations and AB straight
    // from the stored buffer (src/propagation/PropagationAB.cpp:222-281).
    const int mode = h->cfg.prop_pattern == LBM_PATTERN_AA ? logical_mode(h) : 0;
-   double* dr = nullptr;
-   double* du = nullptr;
-   const size_t n = (size_t)h->ncell;
-   lbm_status st = dev_alloc(h, (void**)&dr, sizeof(double) * n);
-   if (st == LBM_OK) st = dev_alloc(h, (void**)&du, sizeof(double) * 3 * n);
-   if (st == LBM_OK) {
-      dispatch_q_st<Macros>(h->Q, h->storage, h, readout_buffer(h), mode, dr, du);
-      cudaError_t e = cudaGetLastError();
-      if (e == cudaSuccess) e = cudaMemcpyAsync(rho, dr, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(u, du, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, h->stream);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-      if (e != cudaSuccess) st = cuda_fail(h, e, "lbm_get_macros");
+   lbm_status st = ensure_copy_stream(h);
+   if (st != LBM_OK) return st;
+   const int64_t n = h->ncell;
+   const int64_t chunk = chunk_cells(h, 4);
+   const size_t half = h->staging_elems / 2;
+   const void* buf = readout_buffer(h);
+   for (int64_t c0 = 0, k = 0; c0 < n; c0 += chunk, k++) {
+      const int64_t cnt = std::min<int64_t>(chunk, n - c0);
+      const int b = (int)(k & 1);
+      double* part = h->staging + b * half;
+      // the half is reused once its previous chunk has reached the host
+      if (k >= 2) LBM_CUDA(h, cudaStreamWaitEvent(h->stream, h->chunk_free[b], 0));
+      dispatch_q_st<Macros>(h->Q, h->storage, h, c0, cnt, buf, mode, part, part + cnt, cnt);
+      LBM_CUDA(h, cudaGetLastError());
+      LBM_CUDA(h, cudaEventRecord(h->chunk_ready[b], h->stream));
+      LBM_CUDA(h, cudaStreamWaitEvent(h->copy_stream, h->chunk_ready[b], 0));
+      LBM_CUDA(h, cudaMemcpyAsync(rho + c0, part, sizeof(double) * cnt, cudaMemcpyDeviceToHost, h->copy_stream));
+      for (int d = 0; d < 3; d++)
+         LBM_CUDA(h, cudaMemcpyAsync(u + (size_t)d * n + c0, part + (1 + d) * cnt, sizeof(double) * cnt,
+                                     cudaMemcpyDeviceToHost, h->copy_stream));
+      LBM_CUDA(h, cudaEventRecord(h->chunk_free[b], h->copy_stream));
    }
-   dev_free(h, dr, sizeof(double) * n);
-   dev_free(h, du, sizeof(double) * 3 * n);
-   return st;
+   cudaError_t e = cudaStreamSynchronize(h->copy_stream);
+   if (e != cudaSuccess) return cuda_fail(h, e, "lbm_get_macros");
+   return LBM_OK;
 }
 
 lbm_status lbm_reduce_conserved(lbm_handle* h, double out[4])

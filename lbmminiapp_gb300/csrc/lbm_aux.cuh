@@ -83,30 +83,54 @@ __device__ __forceinline__ void store_pop(void* buf, int64_t idx, double f, doub
    }
 }
 
-// Reference equilibrium w rho (1 + cu + cu^2/2 - uu/2)
-// (src/kernels/KernelAA_SOA_Base.cpp:229-236), rho/u default to 1/0.
-template <int Q, int ST>
-__global__ void init_eq_kernel(GridDims g, const double* rho, const double* u, void* b0, void* b1,
-                               int aa)
+// Signed sum c_0 a_0 + c_1 a_1 + c_2 a_2 for the compile-time direction S,
+// with the zero terms left out and c = +-1 as an add or subtract: the same
+// value as the reference's c . a (adding +-0 to a sum, or multiplying by
+// +-1, is exact).
+template <int Q, int S>
+__device__ __forceinline__ double cdot_d(double a0, double a1, double a2)
 {
-   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-   if (c >= g.ncell) return;
-   const double r = rho ? rho[c] : 1.0;
-   const double u0 = u ? u[c] : 0.0, u1 = u ? u[g.ncell + c] : 0.0, u2 = u ? u[2 * g.ncell + c] : 0.0;
-   const double uu = 3.0 * (u0 * u0 + u1 * u1 + u2 * u2);
-#pragma unroll
-   for (int s = 0; s < Q; s++) {
-      const double cu = 3.0 * (lat_c(Q, s, 0) * u0 + lat_c(Q, s, 1) * u1 + lat_c(Q, s, 2) * u2);
-      const double w = lat_w(Q, s);
-      const double f = w * r * (1.0 + cu + 0.5 * cu * cu - 0.5 * uu);
+   constexpr int c0 = lat_c(Q, S, 0), c1 = lat_c(Q, S, 1), c2 = lat_c(Q, S, 2);
+   double r = 0.0;
+   if (c0 != 0) r = c0 > 0 ? a0 : -a0;
+   if (c1 != 0) r = c0 != 0 ? (c1 > 0 ? r + a1 : r - a1) : (c1 > 0 ? a1 : -a1);
+   if (c2 != 0) r = (c0 != 0 || c1 != 0) ? (c2 > 0 ? r + a2 : r - a2) : (c2 > 0 ? a2 : -a2);
+   return r;
+}
+
+template <int Q, int ST, int S = 0>
+__device__ __forceinline__ void init_eq_dirs(const GridDims& g, int64_t c, double r, double u0, double u1,
+                                             double u2, double huu, void* b0, void* b1, int aa)
+{
+   if constexpr (S < Q) {
+      const double cu = 3.0 * cdot_d<Q, S>(u0, u1, u2);
+      constexpr double w = lat_w(Q, S);
+      const double f = w * r * (1.0 + cu + 0.5 * cu * cu - huu);
       if (aa) {
-         const int o = lat_opp(Q, s);
+         constexpr int o = lat_opp(Q, S);
          store_pop<ST>(b0, (int64_t)o * g.plane + c, f, lat_w(Q, o));
       } else {
-         store_pop<ST>(b0, (int64_t)s * g.plane + c, f, w);
-         store_pop<ST>(b1, (int64_t)s * g.plane + c, f, w);
+         store_pop<ST>(b0, (int64_t)S * g.plane + c, f, w);
+         store_pop<ST>(b1, (int64_t)S * g.plane + c, f, w);
       }
+      init_eq_dirs<Q, ST, S + 1>(g, c, r, u0, u1, u2, huu, b0, b1, aa);
    }
+}
+
+// Reference equilibrium w rho (1 + cu + cu^2/2 - uu/2)
+// (src/kernels/KernelAA_SOA_Base.cpp:229-236) for the cells [c0, c0+count);
+// rho[k] and u[d*in_stride + k] hold cell c0+k, and default to 1 / 0.
+template <int Q, int ST>
+__global__ void init_eq_kernel(GridDims g, int64_t c0, int64_t count, const double* rho, const double* u,
+                               int64_t in_stride, void* b0, void* b1, int aa)
+{
+   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+   if (k >= count) return;
+   const int64_t c = c0 + k;
+   const double r = rho ? rho[k] : 1.0;
+   const double u0 = u ? u[k] : 0.0, u1 = u ? u[in_stride + k] : 0.0, u2 = u ? u[2 * in_stride + k] : 0.0;
+   const double uu = 3.0 * (u0 * u0 + u1 * u1 + u2 * u2);
+   init_eq_dirs<Q, ST>(g, c, r, u0, u1, u2, 0.5 * uu, b0, b1, aa);
 }
 
 // One direction plane from a dense double plane into slot `slot` of up to two
@@ -166,35 +190,43 @@ __device__ __forceinline__ double logical_pop(const GridDims& g, const void* buf
    return load_pop<ST>(buf, (int64_t)s * g.plane + n, lat_w(Q, s));
 }
 
-// rho and u = sum(c f)/rho (no F/2 shift) per cell; NaN at solid cells.
+// rho and u = sum(c f)/rho (no F/2 shift) for the cells [c0, c0+count);
+// cell c0+k goes to rho[k] and u[d*out_stride + k]; NaN at solid cells.
+// Zero stencil terms are left out and +-1 terms become adds or subtracts,
+// which gives the same sums as the reference's f * c accumulation.
 template <int Q, int ST>
-__global__ void macros_kernel(GridDims g, const void* buf, const uint32_t* links, int mode, double* rho,
-                              double* u)
+__global__ void macros_kernel(GridDims g, int64_t c0, int64_t count, const void* buf, const uint32_t* links,
+                              int mode, double* rho, double* u, int64_t out_stride)
 {
-   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+   if (k >= count) return;
+   const int64_t c = c0 + k;
    int x, y, z;
    if (!cell_xyz(g, c, x, y, z)) return;
    const uint32_t lk = links ? links[c] : 0u;
    if (lk & kSolidBit) {
       const double nan = __longlong_as_double(0x7FF8000000000000LL);
-      rho[c] = nan;
-      u[c] = u[g.ncell + c] = u[2 * g.ncell + c] = nan;
+      rho[k] = nan;
+      u[k] = u[out_stride + k] = u[2 * out_stride + k] = nan;
       return;
    }
-   double r = 0.0, m0 = 0.0, m1 = 0.0, m2 = 0.0;
+   double r = 0.0, m[3] = {0.0, 0.0, 0.0};
 #pragma unroll
    for (int s = 0; s < Q; s++) {
       const double f = logical_pop<Q, ST>(g, buf, lk, x, y, z, c, s, mode);
       r += f;
-      m0 += f * lat_c(Q, s, 0);
-      m1 += f * lat_c(Q, s, 1);
-      m2 += f * lat_c(Q, s, 2);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+         const int cd = lat_c(Q, s, d);
+         if (cd > 0) m[d] += f;
+         else if (cd < 0) m[d] -= f;
+      }
    }
    const double ir = 1.0 / r;
-   rho[c] = r;
-   u[c] = m0 * ir;
-   u[g.ncell + c] = m1 * ir;
-   u[2 * g.ncell + c] = m2 * ir;
+   rho[k] = r;
+   u[k] = m[0] * ir;
+   u[out_stride + k] = m[1] * ir;
+   u[2 * out_stride + k] = m[2] * ir;
 }
 
 // FP64 mass / momentum sums over fluid cells.  Each block reduces its cells
