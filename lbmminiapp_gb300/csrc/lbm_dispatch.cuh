@@ -16,7 +16,7 @@ struct Launch {
    bool idx32;   // plane stride below 2^32 bytes: 32-bit stride arithmetic
    bool pair;    // two cells per thread (shifted storage, periodic box, even nx, full grid)
    dim3 pair_grid, pair_block;
-   bool async;   // pipelined persistent kernel (FP64 storage, F64X, nx % 32 == 0, full grid)
+   bool async;   // pipelined persistent kernel (FP64 storage, F64X, full grid, 32-bit plane stride)
    AsyncGeom ag;
 };
 
@@ -35,7 +35,13 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
       }
    }
    if constexpr (ST == ST_F64 && AR == AR_F64X) {
-      if (L.async && !links && !fields) return launch_async<Q, KIND>(p, L.ag, src, dst, L.stream);
+      if (L.async && !fields) {
+         const bool ragged = p.nx % 32 != 0;
+         if (links) return ragged ? launch_async<Q, KIND, true, true>(p, L.ag, src, dst, L.stream)
+                                  : launch_async<Q, KIND, true, false>(p, L.ag, src, dst, L.stream);
+         return ragged ? launch_async<Q, KIND, false, true>(p, L.ag, src, dst, L.stream)
+                       : launch_async<Q, KIND, false, false>(p, L.ag, src, dst, L.stream);
+      }
    }
    // Per-cell fields always use the exact FP64 arithmetic when FP64 is stored.
    constexpr int ARF = (AR == AR_F64X) ? AR_F64 : AR;

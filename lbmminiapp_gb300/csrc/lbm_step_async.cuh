@@ -1,5 +1,5 @@
-// Software-pipelined step kernel for FP64 storage with F64X arithmetic in a
-// fully periodic box (no link words, no per-cell fields).
+// Software-pipelined step kernel for FP64 storage with F64X arithmetic (any
+// box; link words for walls and solids; no per-cell fields).
 //
 // The F64X collision is about 1.7k instructions per cell, so the plain
 // one-cell-per-thread kernel spends its time either issuing or waiting on its
@@ -13,7 +13,8 @@
 //
 // AA (in place) stays race-free under the prefetch: the locations a cell's
 // thread reads are exactly the ones it writes (even step: its own slots; odd
-// step: slot s at x - c_s and slot opp(s) at x + c_s form the same set), so a
+// step: slot s at x - c_s and slot opp(s) at x + c_s form the same set, a
+// bounced-back direction reading and writing the own cell), so a
 // prefetch of another tile never sees a write of this one.
 #pragma once
 
@@ -31,7 +32,7 @@ constexpr size_t async_smem_bytes()
 }
 
 // Tiles of 32 cells: tile t covers x in [32 (t mod ntx), +32) of row t / ntx,
-// row r = y + ny z.  Divisions by a run-time d use q = umulhi64(n, m) with
+// row r = y + ny z, with ntx = ceil(nx / 32) (lanes past the row end idle).  Divisions by a run-time d use q = umulhi64(n, m) with
 // m = ceil(2^64 / d) (exact for n, d < 2^32); d = 1 is m = 0.
 struct AsyncGeom {
    uint32_t ntiles, ntx;
@@ -43,7 +44,8 @@ __device__ __forceinline__ uint32_t div_magic(uint32_t n, uint32_t d, uint64_t m
    return m ? (uint32_t)__umul64hi((uint64_t)n, m) : n;
 }
 
-__device__ __forceinline__ void tile_cell(const KParams& p, const AsyncGeom& ag, uint32_t t, int lane,
+// Returns false for a lane past the end of its row.
+__device__ __forceinline__ bool tile_cell(const KParams& p, const AsyncGeom& ag, uint32_t t, int lane,
                                           CellIndex& ci)
 {
    const uint32_t row = div_magic(t, ag.ntx, ag.m_ntx);
@@ -58,6 +60,7 @@ __device__ __forceinline__ void tile_cell(const KParams& p, const AsyncGeom& ag,
    const int nxy = p.nx * p.ny;
    ci.dzm = (z == 0) ? (p.nz - 1) * nxy : -nxy;
    ci.dzp = ((int)z == p.nz - 1) ? -(p.nz - 1) * nxy : nxy;
+   return x < p.nx;
 }
 
 __device__ __forceinline__ void cp_async8(uint32_t smem, const void* g)
@@ -77,18 +80,48 @@ struct PlanePtrs {
    unsigned long long* dst[27];
 };
 
-template <int Q, int KIND>
-__device__ __forceinline__ void async_issue(const PlanePtrs& pp, const CellIndex& ci, int lane, uint32_t sbuf)
+// Lane state of a tile: its cell, its link word (0 without walls) and
+// whether it updates anything (inside the row, not solid).
+struct TileLane {
+   CellIndex ci;
+   uint32_t lk;
+   bool active;
+};
+
+// Link word of this lane's cell in tile t (the solid bit past the row end).
+__device__ __forceinline__ uint32_t tile_link(const KParams& p, const AsyncGeom& ag, uint32_t t, int lane)
 {
-   const uint32_t c = (uint32_t)ci.c;
+   const uint32_t row = div_magic(t, ag.ntx, ag.m_ntx);
+   const int x = (int)(t - row * ag.ntx) * 32 + lane;
+   return x < p.nx ? __ldg(p.links + (int64_t)row * p.nx + x) : kSolidBit;
+}
+
+// lk: the tile's link words, loaded one tile ahead so the load's latency
+// hides behind a collision.
+// RAGGED: nx is not a multiple of 32, so some lanes fall past their row.
+template <bool LINKS, bool RAGGED>
+__device__ __forceinline__ void tile_lane(const KParams& p, const AsyncGeom& ag, uint32_t t, int lane, uint32_t lk,
+                                          TileLane& tl)
+{
+   const bool inside = tile_cell(p, ag, t, lane, tl.ci);
+   tl.active = RAGGED ? inside : true;
+   tl.lk = LINKS ? lk : 0u;
+   if (LINKS) tl.active = tl.active && !(lk & kSolidBit);
+}
+
+template <int Q, int KIND, bool LINKS, bool RAGGED>
+__device__ __forceinline__ void async_issue(const PlanePtrs& pp, const TileLane& tl, int lane, uint32_t sbuf)
+{
+   if ((LINKS || RAGGED) && !tl.active) return;
+   const uint32_t c = (uint32_t)tl.ci.c;
 #pragma unroll
    for (int s = 0; s < Q; s++) {
-      const Access a = read_access<Q, KIND, false>(ci, 0u, s);
+      const Access a = read_access<Q, KIND, LINKS>(tl.ci, tl.lk, s);
       cp_async8(sbuf + (uint32_t)(s * 32 + lane) * 8u, pp.src[a.slot] + (c + (uint32_t)a.off));
    }
 }
 
-template <int Q, int KIND>
+template <int Q, int KIND, bool LINKS, bool RAGGED>
 __global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KParams p, const AsyncGeom ag,
                                                                       const PlanePtrs pp)
 {
@@ -101,30 +134,34 @@ __global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KPar
    unsigned long long* mine = async_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 8;
-   CellIndex cur;
-   tile_cell(p, ag, t, lane, cur);
-   async_issue<Q, KIND>(pp, cur, lane, sbase);
+   TileLane cur;
+   tile_lane<LINKS, RAGGED>(p, ag, t, lane, LINKS ? tile_link(p, ag, t, lane) : 0u, cur);
+   uint32_t lk_ahead = (LINKS && t + nw < ag.ntiles) ? tile_link(p, ag, t + nw, lane) : 0u;
+   async_issue<Q, KIND, LINKS, RAGGED>(pp, cur, lane, sbase);
    cp_async_commit();
    int stage = 0;
    for (;;) {
       const uint32_t next = t + nw;
-      CellIndex nxt = cur;
+      TileLane nxt = cur;
       if (next < ag.ntiles) {
-         tile_cell(p, ag, next, lane, nxt);
-         async_issue<Q, KIND>(pp, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
+         tile_lane<LINKS, RAGGED>(p, ag, next, lane, lk_ahead, nxt);
+         if (LINKS && next + nw < ag.ntiles) lk_ahead = tile_link(p, ag, next + nw, lane);
+         async_issue<Q, KIND, LINKS, RAGGED>(pp, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
       }
       cp_async_commit();
       cp_async_wait_prev();
-      uint64_t bits[Q];
-      const unsigned long long* sm = mine + stage * Q * 32;
+      if (!(LINKS || RAGGED) || cur.active) {
+         uint64_t bits[Q];
+         const unsigned long long* sm = mine + stage * Q * 32;
 #pragma unroll
-      for (int s = 0; s < Q; s++) bits[s] = sm[s * 32 + lane];
-      collide_f64x<Q>(bits, p);
-      const uint32_t c = (uint32_t)cur.c;
+         for (int s = 0; s < Q; s++) bits[s] = sm[s * 32 + lane];
+         collide_f64x<Q>(bits, p);
+         const uint32_t c = (uint32_t)cur.ci.c;
 #pragma unroll
-      for (int s = 0; s < Q; s++) {
-         const Access a = write_access<Q, KIND, false>(cur, 0u, s);
-         pp.dst[a.slot][c + (uint32_t)a.off] = bits[s];
+         for (int s = 0; s < Q; s++) {
+            const Access a = write_access<Q, KIND, LINKS>(cur.ci, cur.lk, s);
+            pp.dst[a.slot][c + (uint32_t)a.off] = bits[s];
+         }
       }
       if (next >= ag.ntiles) break;
       t = next;
@@ -136,7 +173,7 @@ __global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KPar
 inline AsyncGeom async_geom(int nx, int ny, int nz)
 {
    AsyncGeom g;
-   g.ntx = (uint32_t)(nx / 32);
+   g.ntx = (uint32_t)((nx + 31) / 32);
    g.ntiles = g.ntx * (uint32_t)ny * (uint32_t)nz;
    g.m_ntx = g.ntx == 1 ? 0 : (~0ull / g.ntx) + 1;
    g.m_ny = ny == 1 ? 0 : (~0ull / (uint64_t)ny) + 1;
@@ -145,7 +182,7 @@ inline AsyncGeom async_geom(int nx, int ny, int nz)
 
 // Persistent grid: as many blocks as fit on the device at once (queried once
 // per device and kernel; the shared-memory opt-in is set at the same time).
-template <int Q, int KIND>
+template <int Q, int KIND, bool LINKS, bool RAGGED>
 cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src, void* dst, cudaStream_t stream)
 {
    static int grid_of_device[64] = {0};
@@ -153,7 +190,7 @@ cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src,
    cudaError_t e = cudaGetDevice(&dev);
    if (e != cudaSuccess) return e;
    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-   auto kern = step_async_kernel<Q, KIND>;
+   auto kern = step_async_kernel<Q, KIND, LINKS, RAGGED>;
    constexpr size_t smem = async_smem_bytes<Q>();
    if (grid_of_device[dev] == 0) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
