@@ -7,6 +7,7 @@
 
 #include "lbm_step.cuh"
 #include "lbm_step_async.cuh"
+#include "lbm_step_async_low.cuh"
 
 namespace lbm {
 
@@ -17,6 +18,7 @@ struct Launch {
    bool pair;    // two cells per thread (shifted storage, periodic box, even nx, full grid)
    dim3 pair_grid, pair_block;
    bool async;   // pipelined persistent kernel (FP64 storage, F64X, full grid, 32-bit plane stride)
+   bool async_low;   // pipelined persistent kernel for shifted storage (full grid, 32-bit plane stride)
    AsyncGeom ag;
 };
 
@@ -28,6 +30,11 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
    const T* s = static_cast<const T*>(src);
    T* d = static_cast<T*>(dst);
    if constexpr (ST != ST_F64) {
+      if (L.async_low && links && !fields) {
+         const bool ragged = p.nx % 32 != 0;
+         return ragged ? launch_async_low<Q, ST, KIND, true, true>(p, L.ag, src, dst, L.stream)
+                       : launch_async_low<Q, ST, KIND, true, false>(p, L.ag, src, dst, L.stream);
+      }
       if (L.pair && !links && !fields) {
          if (L.idx32) step_pair_kernel<Q, ST, KIND, uint32_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
          else step_pair_kernel<Q, ST, KIND, int64_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);

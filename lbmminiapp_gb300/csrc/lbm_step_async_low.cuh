@@ -1,0 +1,168 @@
+// Software-pipelined step kernel for the shifted FP32 / BF16 / FP16 storage
+// (FP32 collision), for any box: link words for walls and solids, rows of
+// any length, no per-cell fields.
+//
+// Same scheme as the FP64 pipelined kernel (lbm_step_async.cuh): persistent
+// warps on tiles of 32 consecutive cells of one x row, one cell per lane;
+// while a warp collides tile k, the populations of tile k+1 are already in
+// flight as cp.async copies into the warp's two-stage shared-memory buffer.
+// cp.async moves 4, 8 or 16 bytes, so each lane copies the aligned 4-byte
+// word that holds its element: the element itself for FP32, the word with
+// the element in its low or high half for 16-bit storage (the half is kept
+// as one bit per direction).  Two lanes may copy the same word; each thread
+// reads back only its own copies, so cp.async.wait_group is the only
+// synchronisation.  Stores go straight from registers.
+//
+// AA stays race-free under the prefetch for the reason given in
+// lbm_step_async.cuh: the locations a cell reads are the ones it writes.
+#pragma once
+
+#include "lbm_step_async.cuh"
+
+namespace lbm {
+
+constexpr int kAsyncLowWarps = 8;
+
+template <int Q>
+constexpr size_t async_low_smem_bytes()
+{
+   return (size_t)kAsyncLowWarps * kAsyncStages * Q * 32 * sizeof(uint32_t);
+}
+
+__device__ __forceinline__ void cp_async4(uint32_t smem, const void* g)
+{
+   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem), "l"(g) : "memory");
+}
+
+// Direction-plane base pointers in the parameter bank (see PlanePtrs).
+template <typename T>
+struct PlanePtrsT {
+   const T* src[27];
+   T* dst[27];
+};
+
+// Raw stored value (S (f - w), as a float) from the copied word.
+template <int ST>
+__device__ __forceinline__ float word_value(uint32_t w, bool high)
+{
+   if constexpr (ST == ST_F32) {
+      return __uint_as_float(w);
+   } else {
+      const unsigned short b = (unsigned short)(high ? (w >> 16) : (w & 0xFFFFu));
+      if constexpr (ST == ST_F16) return __half2float(__ushort_as_half(b));
+      else return __bfloat162float(__ushort_as_bfloat16(b));
+   }
+}
+
+// Issue the copies of one lane's populations; returns the word-half mask
+// (bit s set: direction s sits in the high half of its word).
+template <int Q, int ST, int KIND, bool LINKS, bool RAGGED>
+__device__ __forceinline__ uint32_t async_issue_low(const PlanePtrsT<typename Store<ST>::T>& pp, const TileLane& tl,
+                                                    int lane, uint32_t sbuf)
+{
+   using T = typename Store<ST>::T;
+   uint32_t halves = 0u;
+   if ((LINKS || RAGGED) && !tl.active) return halves;
+   const uint32_t c = (uint32_t)tl.ci.c;
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      const Access a = read_access<Q, KIND, LINKS>(tl.ci, tl.lk, s);
+      const uint32_t e = c + (uint32_t)a.off;
+      const T* elem = pp.src[a.slot] + e;
+      const void* word = elem;
+      if constexpr (sizeof(T) == 2) {
+         word = reinterpret_cast<const void*>(reinterpret_cast<uintptr_t>(elem) & ~(uintptr_t)3);
+         halves |= (e & 1u) << s;
+      }
+      cp_async4(sbuf + (uint32_t)(s * 32 + lane) * 4u, word);
+   }
+   return halves;
+}
+
+template <int Q, int ST, int KIND, bool LINKS, bool RAGGED>
+__global__ void __launch_bounds__(kAsyncLowWarps * 32) step_async_low_kernel(
+   const KParams p, const AsyncGeom ag, const PlanePtrsT<typename Store<ST>::T> pp)
+{
+   extern __shared__ __align__(16) uint32_t async_low_smem[];
+   const int lane = threadIdx.x & 31;
+   const int warp = threadIdx.x >> 5;
+   const uint32_t nw = gridDim.x * kAsyncLowWarps;
+   uint32_t t = blockIdx.x * kAsyncLowWarps + warp;
+   if (t >= ag.ntiles) return;
+   uint32_t* mine = async_low_smem + (size_t)warp * kAsyncStages * Q * 32;
+   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
+   constexpr uint32_t kStageBytes = Q * 32 * 4;
+   TileLane cur;
+   tile_lane<LINKS, RAGGED>(p, ag, t, lane, LINKS ? tile_link(p, ag, t, lane) : 0u, cur);
+   uint32_t lk_ahead = (LINKS && t + nw < ag.ntiles) ? tile_link(p, ag, t + nw, lane) : 0u;
+   uint32_t halves = async_issue_low<Q, ST, KIND, LINKS, RAGGED>(pp, cur, lane, sbase);
+   cp_async_commit();
+   int stage = 0;
+   for (;;) {
+      const uint32_t next = t + nw;
+      TileLane nxt = cur;
+      uint32_t halves_next = 0u;
+      if (next < ag.ntiles) {
+         tile_lane<LINKS, RAGGED>(p, ag, next, lane, lk_ahead, nxt);
+         if (LINKS && next + nw < ag.ntiles) lk_ahead = tile_link(p, ag, next + nw, lane);
+         halves_next = async_issue_low<Q, ST, KIND, LINKS, RAGGED>(pp, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
+      }
+      cp_async_commit();
+      cp_async_wait_prev();
+      if (!(LINKS || RAGGED) || cur.active) {
+         float g[Q], o[Q];
+         const uint32_t* sm = mine + stage * Q * 32;
+#pragma unroll
+         for (int s = 0; s < Q; s++) g[s] = word_value<ST>(sm[s * 32 + lane], (halves >> s) & 1u);
+         if (p.forced) collide_f32<Q, ST, true>(g, o, p.Ff[0], p.Ff[1], p.Ff[2], 0.0f, p);
+         else collide_f32<Q, ST, false>(g, o, 0.0f, 0.0f, 0.0f, 0.0f, p);
+         const uint32_t c = (uint32_t)cur.ci.c;
+#pragma unroll
+         for (int s = 0; s < Q; s++) {
+            const Access a = write_access<Q, KIND, LINKS>(cur.ci, cur.lk, s);
+            store_raw(pp.dst[a.slot] + (c + (uint32_t)a.off), o[s]);
+         }
+      }
+      if (next >= ag.ntiles) break;
+      t = next;
+      cur = nxt;
+      halves = halves_next;
+      stage ^= 1;
+   }
+}
+
+template <int Q, int ST, int KIND, bool LINKS, bool RAGGED>
+cudaError_t launch_async_low(const KParams& p, const AsyncGeom& ag, const void* src, void* dst, cudaStream_t stream)
+{
+   using T = typename Store<ST>::T;
+   static int grid_of_device[64] = {0};
+   int dev = 0;
+   cudaError_t e = cudaGetDevice(&dev);
+   if (e != cudaSuccess) return e;
+   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+   auto kern = step_async_low_kernel<Q, ST, KIND, LINKS, RAGGED>;
+   constexpr size_t smem = async_low_smem_bytes<Q>();
+   if (grid_of_device[dev] == 0) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      int per_sm = 0, nsm = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kAsyncLowWarps * 32, smem);
+      if (e != cudaSuccess) return e;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      if (per_sm < 1) return cudaErrorInvalidConfiguration;
+      grid_of_device[dev] = per_sm * nsm;
+   }
+   const uint32_t need = (ag.ntiles + kAsyncLowWarps - 1) / kAsyncLowWarps;
+   const unsigned grid = (unsigned)(need < (uint32_t)grid_of_device[dev] ? need : (uint32_t)grid_of_device[dev]);
+   PlanePtrsT<T> pp;
+   for (int s = 0; s < 27; s++) {
+      const int k = s < Q ? s : 0;
+      pp.src[s] = static_cast<const T*>(src) + (int64_t)k * p.plane;
+      pp.dst[s] = static_cast<T*>(dst) + (int64_t)k * p.plane;
+   }
+   kern<<<grid, kAsyncLowWarps * 32, smem, stream>>>(p, ag, pp);
+   return cudaGetLastError();
+}
+
+}  // namespace lbm
