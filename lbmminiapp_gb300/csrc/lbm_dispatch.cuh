@@ -30,14 +30,9 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
    const T* s = static_cast<const T*>(src);
    T* d = static_cast<T*>(dst);
    if constexpr (ST != ST_F64) {
-      if (L.pair && !fields) {
-         if (links) {
-            if (L.idx32) step_pair_kernel<Q, ST, KIND, true, uint32_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
-            else step_pair_kernel<Q, ST, KIND, true, int64_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
-         } else {
-            if (L.idx32) step_pair_kernel<Q, ST, KIND, false, uint32_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
-            else step_pair_kernel<Q, ST, KIND, false, int64_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
-         }
+      if (L.pair && !links && !fields) {
+         if (L.idx32) step_pair_kernel<Q, ST, KIND, uint32_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
+         else step_pair_kernel<Q, ST, KIND, int64_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
          return cudaGetLastError();
       }
       if (L.async_low && links && !fields) {

@@ -184,10 +184,10 @@ __global__ void __launch_bounds__(256) step_kernel(const KParams p, const typena
 }
 
 // ------------------------------------------------------------------------
-// Two cells per thread (x0, x0+1) for shifted FP32/BF16/FP16 storage: planes
-// not shifted along x are read and written as one aligned 2-element vector
-// (half2 / bfloat162 / float2); x-shifted planes use two scalar accesses.
-// Requires an even nx and a full-grid launch.
+// Two cells per thread (x0, x0+1) for shifted FP32/BF16/FP16 storage in a
+// fully periodic box: planes not shifted along x are read and written as one
+// aligned 2-element vector (half2 / bfloat162 / float2); x-shifted planes use
+// two scalar accesses.  Requires an even nx and a full-grid launch.
 template <typename T> struct PairVec;
 template <> struct PairVec<float> {
    using V = float2;
@@ -229,7 +229,7 @@ __device__ constexpr bool write_shifted_x(int s)
    return (KIND == K_AA_ODD || KIND == K_AB_PUSH) && s != lat_rest(Q) && lat_c(Q, s, 0) != 0;
 }
 
-template <int Q, int ST, int KIND, bool LINKS, typename IT>
+template <int Q, int ST, int KIND, typename IT>
 __global__ void __launch_bounds__(256) step_pair_kernel(const KParams p, const typename Store<ST>::T* src,
                                                         typename Store<ST>::T* dst)
 {
@@ -241,19 +241,6 @@ __global__ void __launch_bounds__(256) step_pair_kernel(const KParams p, const t
    CellIndex c0, c1;
    cell_offsets(p, x0, y, z, c0);
    cell_offsets(p, x0 + 1, y, z, c1);
-   // With walls: a solid cell of the pair does nothing; a direction whose
-   // streaming the two cells share (both free or both bounced back, and no
-   // shift along x) moves as one vector, otherwise as two scalars.
-   uint32_t lk0 = 0u, lk1 = 0u;
-   bool on0 = true, on1 = true;
-   if (LINKS) {
-      const uint2 lk = *reinterpret_cast<const uint2*>(p.links + c0.c);   // c0.c is even
-      lk0 = lk.x;
-      lk1 = lk.y;
-      on0 = !(lk0 & kSolidBit);
-      on1 = !(lk1 & kSolidBit);
-      if (!on0 && !on1) return;
-   }
    const IT pb = (IT)p.plane * (IT)sizeof(T);
    const T* s0 = src + c0.c;
    const T* s1 = src + c1.c;
@@ -262,17 +249,15 @@ __global__ void __launch_bounds__(256) step_pair_kernel(const KParams p, const t
    float g0[Q], g1[Q], o0[Q], o1[Q];
 #pragma unroll
    for (int s = 0; s < Q; s++) {
-      const Access a0 = read_access<Q, KIND, LINKS>(c0, lk0, s);
-      const Access a1 = read_access<Q, KIND, LINKS>(c1, lk1, s);
-      const bool vec = read_shifted_x<Q, KIND>(s) ? (LINKS && on0 && on1 && a0.off == 0 && a1.off == 0)
-                                                  : (!LINKS || (on0 && on1 && a0.slot == a1.slot));
-      if (vec) {
+      const Access a0 = read_access<Q, KIND, false>(c0, 0u, s);
+      if (read_shifted_x<Q, KIND>(s)) {
+         const Access a1 = read_access<Q, KIND, false>(c1, 0u, s);
+         g0[s] = load_raw(slot_ptr(s0, pb, a0));
+         g1[s] = load_raw(slot_ptr(s1, pb, a1));
+      } else {
          const float2 v = PV::get(*reinterpret_cast<const typename PV::V*>(slot_ptr(s0, pb, a0)));
          g0[s] = v.x;
          g1[s] = v.y;
-      } else {
-         g0[s] = on0 ? load_raw(slot_ptr(s0, pb, a0)) : 0.0f;
-         g1[s] = on1 ? load_raw(slot_ptr(s1, pb, a1)) : 0.0f;
       }
    }
    if (p.forced) {
@@ -284,15 +269,13 @@ __global__ void __launch_bounds__(256) step_pair_kernel(const KParams p, const t
    }
 #pragma unroll
    for (int s = 0; s < Q; s++) {
-      const Access a0 = write_access<Q, KIND, LINKS>(c0, lk0, s);
-      const Access a1 = write_access<Q, KIND, LINKS>(c1, lk1, s);
-      const bool vec = write_shifted_x<Q, KIND>(s) ? (LINKS && on0 && on1 && a0.off == 0 && a1.off == 0)
-                                                   : (!LINKS || (on0 && on1 && a0.slot == a1.slot));
-      if (vec) {
-         *reinterpret_cast<typename PV::V*>(slot_ptr(d0, pb, a0)) = PV::put(o0[s], o1[s]);
+      const Access a0 = write_access<Q, KIND, false>(c0, 0u, s);
+      if (write_shifted_x<Q, KIND>(s)) {
+         const Access a1 = write_access<Q, KIND, false>(c1, 0u, s);
+         store_raw(slot_ptr(d0, pb, a0), o0[s]);
+         store_raw(slot_ptr(d1, pb, a1), o1[s]);
       } else {
-         if (on0) store_raw(slot_ptr(d0, pb, a0), o0[s]);
-         if (on1) store_raw(slot_ptr(d1, pb, a1), o1[s]);
+         *reinterpret_cast<typename PV::V*>(slot_ptr(d0, pb, a0)) = PV::put(o0[s], o1[s]);
       }
    }
 }
