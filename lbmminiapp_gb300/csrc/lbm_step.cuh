@@ -229,8 +229,14 @@ __device__ constexpr bool write_shifted_x(int s)
    return (KIND == K_AA_ODD || KIND == K_AB_PUSH) && s != lat_rest(Q) && lat_c(Q, s, 0) != 0;
 }
 
+// Resident blocks per SM: the kernel waits on its loads, and more resident
+// warps keep more of them in flight.  16-bit storage: four blocks (at most 64
+// registers; measured on GB300, FP16 71 -> 76 GLUPS at 512^3); FP32: three.
+template <int ST>
+constexpr int pair_min_blocks() { return Store<ST>::bytes == 2 ? 4 : 3; }
+
 template <int Q, int ST, int KIND, typename IT>
-__global__ void __launch_bounds__(256) step_pair_kernel(const KParams p, const typename Store<ST>::T* src,
+__global__ void __launch_bounds__(256, pair_min_blocks<ST>()) step_pair_kernel(const KParams p, const typename Store<ST>::T* src,
                                                         typename Store<ST>::T* dst)
 {
    using T = typename Store<ST>::T;
