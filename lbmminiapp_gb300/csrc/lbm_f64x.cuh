@@ -453,25 +453,26 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
 
    // rho and j = sum c_s f_s from the exact sums of the fixed-point images
    // floor(f * 2^53); rho < 2 is checked (rho's top word below 2^22).
-   uint64_t X[Q];
-#pragma unroll
-   for (int s = 0; s < Q; s++) X[s] = fixed53(bits[s]);
+   // One pass: each image goes straight into the four sums.
    uint64_t rho_x = (uint64_t)(Q / 2);   // mean truncation loss, half a unit per population
+   int64_t jx[3] = {0, 0, 0};
 #pragma unroll
-   for (int s = 0; s < Q; s++) rho_x += X[s];
+   for (int s = 0; s < Q; s++) {
+      const uint64_t X = fixed53(bits[s]);
+      rho_x += X;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+         const int c = lat_c(Q, s, d);
+         if (c > 0) jx[d] += (int64_t)X;
+         if (c < 0) jx[d] -= (int64_t)X;
+      }
+   }
    if ((rho_x >> 32) >= (1u << 22)) return false;
    df j[3];
 #pragma unroll
    for (int d = 0; d < 3; d++) {
-      int64_t jx = 0;
-#pragma unroll
-      for (int s = 0; s < Q; s++) {
-         const int c = lat_c(Q, s, d);
-         if (c > 0) jx += (int64_t)X[s];
-         if (c < 0) jx -= (int64_t)X[s];
-      }
       // Fast2Sum is exact here: t.h is 0 or a multiple of 2^-23 above |t.l|.
-      const df t = fixed53_to_pair(jx);
+      const df t = fixed53_to_pair(jx[d]);
       j[d] = fast_two_sum(t.h, t.l);
    }
    // rho >= 1/4 (the rest population alone): Fast2Sum normalises the pair.
@@ -609,7 +610,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
 // F64X cell update with a uniform force: fast path, else the exact IEEE
 // double collision.
 template <int Q>
-__device__ __forceinline__ void collide_f64x(uint64_t (&bits)[Q], const KParams& p)
+__device__ __forceinline__ x64::Consts collide_consts(const KParams& p)
 {
    x64::Consts k;
    k.om1 = {p.x_om1[0], p.x_om1[1]};
@@ -626,15 +627,53 @@ __device__ __forceinline__ void collide_f64x(uint64_t (&bits)[Q], const KParams&
    for (int c = 0; c < 4; c++) k.om2w[c] = {p.x_om2w[c][0], p.x_om2w[c][1]};
    k.om2w36 = {p.x_om2w36[0], p.x_om2w36[1]};
    k.om2 = p.om2f;
-   const bool fast = p.forced ? collide_f64x_fast<Q, true>(bits, k, p.compat)
-                              : collide_f64x_fast<Q, false>(bits, k, p.compat);
-   if (fast) return;
+   return k;
+}
+
+template <int Q>
+__device__ __forceinline__ void collide_exact_bits(uint64_t (&bits)[Q], const KParams& p)
+{
    double d[Q], o[Q];
 #pragma unroll
    for (int s = 0; s < Q; s++) d[s] = x64::as_double(bits[s]);
    collide_f64<Q>(d, o, p.F[0], p.F[1], p.F[2], 0.0, p);
 #pragma unroll
    for (int s = 0; s < Q; s++) bits[s] = x64::double_bits(o[s]);
+}
+
+// F64X cell update with a uniform force: fast path, else the exact IEEE
+// double collision.
+template <int Q>
+__device__ __forceinline__ void collide_f64x(uint64_t (&bits)[Q], const KParams& p)
+{
+   const x64::Consts k = collide_consts<Q>(p);
+   const bool fast = p.forced ? collide_f64x_fast<Q, true>(bits, k, p.compat)
+                              : collide_f64x_fast<Q, false>(bits, k, p.compat);
+   if (fast) return;
+   collide_exact_bits<Q>(bits, p);
+}
+
+// The same for inputs that stay in shared memory (direction s at
+// in[32 s]): the fallback reads them again from there, so the input
+// patterns need not stay in registers through the fast path.
+template <int Q>
+__device__ __forceinline__ void collide_f64x_shared(const unsigned long long* in, uint64_t (&bits)[Q],
+                                                    const KParams& p)
+{
+#pragma unroll
+   for (int s = 0; s < Q; s++) bits[s] = in[s * 32];
+   const x64::Consts k = collide_consts<Q>(p);
+   const bool fast = p.forced ? collide_f64x_fast<Q, true>(bits, k, p.compat)
+                              : collide_f64x_fast<Q, false>(bits, k, p.compat);
+   if (fast) return;
+   const uint32_t a = (uint32_t)__cvta_generic_to_shared(in);
+#pragma unroll
+   for (int s = 0; s < Q; s++) {
+      unsigned long long v;
+      asm volatile("ld.shared.u64 %0, [%1];\n" : "=l"(v) : "r"(a + 256u * (uint32_t)s));
+      bits[s] = v;
+   }
+   collide_exact_bits<Q>(bits, p);
 }
 
 }  // namespace lbm

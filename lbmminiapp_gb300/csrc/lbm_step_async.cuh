@@ -152,10 +152,7 @@ __global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KPar
       cp_async_wait_prev();
       if (!(LINKS || RAGGED) || cur.active) {
          uint64_t bits[Q];
-         const unsigned long long* sm = mine + stage * Q * 32;
-#pragma unroll
-         for (int s = 0; s < Q; s++) bits[s] = sm[s * 32 + lane];
-         collide_f64x<Q>(bits, p);
+         collide_f64x_shared<Q>(mine + stage * Q * 32 + lane, bits, p);
          const uint32_t c = (uint32_t)cur.ci.c;
 #pragma unroll
          for (int s = 0; s < Q; s++) {
