@@ -22,7 +22,7 @@
 
 namespace lbm {
 
-constexpr int kAsyncWarps = 8;   // warps per block
+constexpr int kAsyncWarps = 4;   // warps per block (three blocks per SM: measured best for Q19 and Q27)
 constexpr int kAsyncStages = 2;
 
 template <int Q>
@@ -122,7 +122,7 @@ __device__ __forceinline__ void async_issue(const PlanePtrs& pp, const TileLane&
 }
 
 template <int Q, int KIND, bool LINKS, bool RAGGED>
-__global__ void __launch_bounds__(kAsyncWarps * 32) step_async_kernel(const KParams p, const AsyncGeom ag,
+__global__ void __launch_bounds__(kAsyncWarps * 32, 3) step_async_kernel(const KParams p, const AsyncGeom ag,
                                                                       const PlanePtrs pp)
 {
    extern __shared__ __align__(16) unsigned long long async_smem[];
