@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=1000,
                     help="lattice steps of the end-to-end round trip (the workload's 1000 steps)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ref-n", type=int, default=256, help="box edge of the reference arm's sample")
     ap.add_argument("--storage", default="f64", choices=["f64", "f32", "bf16", "f16"],
                     help="population storage of the timed run (headline: f64)")
     ap.add_argument("--lattice", type=int, default=19, choices=[19, 27])
@@ -314,11 +315,22 @@ def cylinder_benchmark(device, size=8.0, steps=20):
     return out
 
 
+def max_over_ranks(dist, value: float, device) -> float:
+    """The largest `value` over all ranks (every rank gets it); `value` itself
+    without a process group."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference_arm(args, dist, rank, world):
     if rank != 0:
         return 0
     from oracle import core
-    n = 256
+    n = args.ref_n
     u = workload_velocity(n)
     f0 = core.equilibrium(19, np.ones((n, n, n)), u)
     del u
@@ -337,7 +349,7 @@ def run_reference_arm(args, dist, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Taylor-Green + SplitMix64 noise)",
         "config": {"workload": "D3Q19 AA FP64 Taylor-Green periodic box, tau=0.55; each step one lattice "
-                               "step of a 256^3 sample (1/8 of the 512^3 box)", "lattice": "D3Q19",
+                               f"step of a {n}^3 sample of the 512^3 box", "lattice": "D3Q19",
                    "propagation": "AA", "grid": [n, n, n], "storage": "f64"},
         "cpu_baseline": {"value": round(mlups, 3), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n}^3 box, {args.steps} timed lattice steps; oracle/lbm_oracle.c "
@@ -396,9 +408,7 @@ def main():
     per_launch_ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps)]
     total_ms = ev[0].elapsed_time(ev[-1])
     if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+        total_ms = max_over_ranks(dist, total_ms, "cuda")
         dist.barrier()
     value = world * ncell * args.steps / (total_ms * 1e-3) / 1e6
     mass = float(sim.conserved()[0]) / ncell
