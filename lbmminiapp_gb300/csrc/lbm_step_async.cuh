@@ -22,13 +22,20 @@
 
 namespace lbm {
 
-constexpr int kAsyncWarps = 4;   // warps per block (three blocks per SM: measured best for Q19 and Q27)
+// Warps per block and blocks per SM, measured on GB300: the D3Q19 AA even
+// step runs best with 8-warp blocks, two per SM (128 registers); every other
+// kind, and all of D3Q27, with 4-warp blocks, three per SM (at most 170
+// registers).
+template <int Q, int KIND>
+constexpr int async_warps() { return (Q == 19 && KIND == K_AA_EVEN) ? 8 : 4; }
+template <int Q, int KIND>
+constexpr int async_min_blocks() { return async_warps<Q, KIND>() == 8 ? 2 : 3; }
 constexpr int kAsyncStages = 2;
 
-template <int Q>
+template <int Q, int KIND>
 constexpr size_t async_smem_bytes()
 {
-   return (size_t)kAsyncWarps * kAsyncStages * Q * 32 * sizeof(unsigned long long);
+   return (size_t)async_warps<Q, KIND>() * kAsyncStages * Q * 32 * sizeof(unsigned long long);
 }
 
 // Tiles of 32 cells: tile t covers x in [32 (t mod ntx), +32) of row t / ntx,
@@ -122,14 +129,15 @@ __device__ __forceinline__ void async_issue(const PlanePtrs& pp, const TileLane&
 }
 
 template <int Q, int KIND, bool LINKS, bool RAGGED>
-__global__ void __launch_bounds__(kAsyncWarps * 32, 3) step_async_kernel(const KParams p, const AsyncGeom ag,
+__global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<Q, KIND>()) step_async_kernel(const KParams p, const AsyncGeom ag,
                                                                       const PlanePtrs pp)
 {
    extern __shared__ __align__(16) unsigned long long async_smem[];
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
-   const uint32_t nw = gridDim.x * kAsyncWarps;
-   uint32_t t = blockIdx.x * kAsyncWarps + warp;
+   constexpr int kWarps = async_warps<Q, KIND>();
+   const uint32_t nw = gridDim.x * kWarps;
+   uint32_t t = blockIdx.x * kWarps + warp;
    if (t >= ag.ntiles) return;
    unsigned long long* mine = async_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
@@ -188,19 +196,20 @@ cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src,
    if (e != cudaSuccess) return e;
    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
    auto kern = step_async_kernel<Q, KIND, LINKS, RAGGED>;
-   constexpr size_t smem = async_smem_bytes<Q>();
+   constexpr int kWarps = async_warps<Q, KIND>();
+   constexpr size_t smem = async_smem_bytes<Q, KIND>();
    if (grid_of_device[dev] == 0) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
       int per_sm = 0, nsm = 0;
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kAsyncWarps * 32, smem);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kWarps * 32, smem);
       if (e != cudaSuccess) return e;
       e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
       if (e != cudaSuccess) return e;
       if (per_sm < 1) return cudaErrorInvalidConfiguration;
       grid_of_device[dev] = per_sm * nsm;
    }
-   const uint32_t need = (ag.ntiles + kAsyncWarps - 1) / kAsyncWarps;
+   const uint32_t need = (ag.ntiles + kWarps - 1) / kWarps;
    const unsigned grid = (unsigned)(need < (uint32_t)grid_of_device[dev] ? need : (uint32_t)grid_of_device[dev]);
    PlanePtrs pp;
    for (int s = 0; s < 27; s++) {
@@ -208,7 +217,7 @@ cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src,
       pp.src[s] = static_cast<const unsigned long long*>(src) + (int64_t)k * p.plane;
       pp.dst[s] = static_cast<unsigned long long*>(dst) + (int64_t)k * p.plane;
    }
-   kern<<<grid, kAsyncWarps * 32, smem, stream>>>(p, ag, pp);
+   kern<<<grid, kWarps * 32, smem, stream>>>(p, ag, pp);
    return cudaGetLastError();
 }
 
