@@ -65,8 +65,14 @@ lbm_status sfail(lbm_sparse_handle* h, lbm_status s, const char* fmt, ...)
    return s;
 }
 
+// D3Q19: two blocks per SM (at most 128 registers; the AA even step alone
+// wanted 140, which left one block per SM and made it slower than the odd
+// step).
+template <int Q>
+constexpr int sparse_min_blocks() { return Q == 19 ? 2 : 1; }
+
 template <int Q, int AR, int KIND>
-__global__ void __launch_bounds__(kSparseThreads) sparse_step_kernel(const KParams p, const int32_t* __restrict__ adj,
+__global__ void __launch_bounds__(kSparseThreads, sparse_min_blocks<Q>()) sparse_step_kernel(const KParams p, const int32_t* __restrict__ adj,
                                                                      int64_t nfluid, int64_t start, int64_t count,
                                                                      const double* src, double* dst)
 {
