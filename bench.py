@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--porous", action="store_true",
                     help="print the sphere-packing permeability / porosity-gradient study instead of timing")
     ap.add_argument("--porous-n", type=int, default=384)
+    ap.add_argument("--reference-benchmark", action="store_true",
+                    help="print only the reference's cylinder benchmark (compact and dense layouts)")
+    ap.add_argument("--cylinder-size", type=float, default=8.0)
+    ap.add_argument("--cylinder-steps", type=int, default=20)
     ap.add_argument("--porous-steps", type=int, default=2000)
     return ap.parse_args()
 
@@ -381,6 +385,9 @@ def main():
     torch.cuda.set_device(local)
     if args.porous:
         return run_porous(args, local)
+    if args.reference_benchmark:
+        print(json.dumps(cylinder_benchmark(local, args.cylinder_size, args.cylinder_steps)), flush=True)
+        return 0
     n = args.n
     ncell = n ** 3
     Q = args.lattice
