@@ -18,6 +18,8 @@
 // prefetch of another tile never sees a write of this one.
 #pragma once
 
+#include <atomic>
+
 #include "lbm_step.cuh"
 
 namespace lbm {
@@ -190,7 +192,9 @@ inline AsyncGeom async_geom(int nx, int ny, int nz)
 template <int Q, int KIND, bool LINKS, bool RAGGED>
 cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src, void* dst, cudaStream_t stream)
 {
-   static int grid_of_device[64] = {0};
+   // Persistent grid size per device ordinal, set once (the value is the same
+   // whichever thread computes it first).
+   static std::atomic<int> grid_of_device[64];
    int dev = 0;
    cudaError_t e = cudaGetDevice(&dev);
    if (e != cudaSuccess) return e;
@@ -198,7 +202,8 @@ cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src,
    auto kern = step_async_kernel<Q, KIND, LINKS, RAGGED>;
    constexpr int kWarps = async_warps<Q, KIND>();
    constexpr size_t smem = async_smem_bytes<Q, KIND>();
-   if (grid_of_device[dev] == 0) {
+   int cached = grid_of_device[dev].load(std::memory_order_relaxed);
+   if (cached == 0) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
       int per_sm = 0, nsm = 0;
@@ -207,10 +212,11 @@ cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src,
       e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
       if (e != cudaSuccess) return e;
       if (per_sm < 1) return cudaErrorInvalidConfiguration;
-      grid_of_device[dev] = per_sm * nsm;
+      cached = per_sm * nsm;
+      grid_of_device[dev].store(cached, std::memory_order_relaxed);
    }
    const uint32_t need = (ag.ntiles + kWarps - 1) / kWarps;
-   const unsigned grid = (unsigned)(need < (uint32_t)grid_of_device[dev] ? need : (uint32_t)grid_of_device[dev]);
+   const unsigned grid = (unsigned)(need < (uint32_t)cached ? need : (uint32_t)cached);
    PlanePtrs pp;
    for (int s = 0; s < 27; s++) {
       const int k = s < Q ? s : 0;

@@ -135,14 +135,17 @@ template <int Q, int ST, int KIND, bool LINKS, bool RAGGED>
 cudaError_t launch_async_low(const KParams& p, const AsyncGeom& ag, const void* src, void* dst, cudaStream_t stream)
 {
    using T = typename Store<ST>::T;
-   static int grid_of_device[64] = {0};
+   // Persistent grid size per device ordinal, set once (the value is the same
+   // whichever thread computes it first).
+   static std::atomic<int> grid_of_device[64];
    int dev = 0;
    cudaError_t e = cudaGetDevice(&dev);
    if (e != cudaSuccess) return e;
    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
    auto kern = step_async_low_kernel<Q, ST, KIND, LINKS, RAGGED>;
    constexpr size_t smem = async_low_smem_bytes<Q>();
-   if (grid_of_device[dev] == 0) {
+   int cached = grid_of_device[dev].load(std::memory_order_relaxed);
+   if (cached == 0) {
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
       int per_sm = 0, nsm = 0;
@@ -151,10 +154,11 @@ cudaError_t launch_async_low(const KParams& p, const AsyncGeom& ag, const void* 
       e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
       if (e != cudaSuccess) return e;
       if (per_sm < 1) return cudaErrorInvalidConfiguration;
-      grid_of_device[dev] = per_sm * nsm;
+      cached = per_sm * nsm;
+      grid_of_device[dev].store(cached, std::memory_order_relaxed);
    }
    const uint32_t need = (ag.ntiles + kAsyncLowWarps - 1) / kAsyncLowWarps;
-   const unsigned grid = (unsigned)(need < (uint32_t)grid_of_device[dev] ? need : (uint32_t)grid_of_device[dev]);
+   const unsigned grid = (unsigned)(need < (uint32_t)cached ? need : (uint32_t)cached);
    PlanePtrsT<T> pp;
    for (int s = 0; s < 27; s++) {
       const int k = s < Q ? s : 0;
