@@ -30,15 +30,6 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
    const T* s = static_cast<const T*>(src);
    T* d = static_cast<T*>(dst);
    if constexpr (ST != ST_F64) {
-      if constexpr (KIND == K_AA_EVEN) {
-         // the even step touches only the cell's own slots: the pair kernel
-         // serves boxes with solids too
-         if (L.pair && links && !fields) {
-            if (L.idx32) step_pair_kernel<Q, ST, KIND, uint32_t, true><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
-            else step_pair_kernel<Q, ST, KIND, int64_t, true><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
-            return cudaGetLastError();
-         }
-      }
       if (L.pair && !links && !fields) {
          if (L.idx32) step_pair_kernel<Q, ST, KIND, uint32_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
          else step_pair_kernel<Q, ST, KIND, int64_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);

@@ -236,14 +236,10 @@ __device__ constexpr bool write_shifted_x(int s)
 template <int Q, int ST>
 constexpr int pair_min_blocks() { return Q == 27 ? 2 : (Store<ST>::bytes == 2 ? 4 : 3); }
 
-// SOLIDS (AA even step only, whose accesses are all the cell's own slots):
-// the box has solid cells; a solid cell of the pair is computed on whatever
-// its slots hold and not stored.
-template <int Q, int ST, int KIND, typename IT, bool SOLIDS = false>
+template <int Q, int ST, int KIND, typename IT>
 __global__ void __launch_bounds__(256, pair_min_blocks<Q, ST>()) step_pair_kernel(const KParams p, const typename Store<ST>::T* src,
                                                         typename Store<ST>::T* dst)
 {
-   static_assert(!SOLIDS || KIND == K_AA_EVEN, "solid cells in the pair kernel: AA even step only");
    using T = typename Store<ST>::T;
    using PV = PairVec<T>;
    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
@@ -252,13 +248,6 @@ __global__ void __launch_bounds__(256, pair_min_blocks<Q, ST>()) step_pair_kerne
    CellIndex c0, c1;
    cell_offsets(p, x0, y, z, c0);
    cell_offsets(p, x0 + 1, y, z, c1);
-   bool on0 = true, on1 = true;
-   if (SOLIDS) {
-      const uint2 lk = *reinterpret_cast<const uint2*>(p.links + c0.c);   // c0.c is even
-      on0 = !(lk.x & kSolidBit);
-      on1 = !(lk.y & kSolidBit);
-      if (!on0 && !on1) return;
-   }
    const IT pb = (IT)p.plane * (IT)sizeof(T);
    const T* s0 = src + c0.c;
    const T* s1 = src + c1.c;
@@ -292,12 +281,8 @@ __global__ void __launch_bounds__(256, pair_min_blocks<Q, ST>()) step_pair_kerne
          const Access a1 = write_access<Q, KIND, false>(c1, 0u, s);
          store_raw(slot_ptr(d0, pb, a0), o0[s]);
          store_raw(slot_ptr(d1, pb, a1), o1[s]);
-      } else if (!SOLIDS || (on0 && on1)) {
-         *reinterpret_cast<typename PV::V*>(slot_ptr(d0, pb, a0)) = PV::put(o0[s], o1[s]);
-      } else if (on0) {
-         store_raw(slot_ptr(d0, pb, a0), o0[s]);
       } else {
-         store_raw(slot_ptr(d1, pb, write_access<Q, KIND, false>(c1, 0u, s)), o1[s]);
+         *reinterpret_cast<typename PV::V*>(slot_ptr(d0, pb, a0)) = PV::put(o0[s], o1[s]);
       }
    }
 }

@@ -1,9 +1,8 @@
 """Shifted FP32 / BF16 / FP16 storage with walls and solids.
 
-The full-grid step runs the two-cells-per-thread kernel for the AA even step
-when nx is even (its accesses are all own slots) and the pipelined
-one-cell-per-lane kernel otherwise (nx = 14 and 13 cover both); kernel-level
-range calls run the one-cell-per-thread kernel.  Both are checked against the FP64 oracle (the
+The full-grid step runs the pipelined one-cell-per-lane kernel (rows of 32
+cells, full and ragged: nx = 14 and 13); kernel-level range calls run the
+one-cell-per-thread kernel.  Both are checked against the FP64 oracle (the
 tolerance is the storage format's rounding, relative to max |f| over fluid
 cells, after 5 steps) and against each other."""
 import numpy as np
