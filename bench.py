@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--porous-n", type=int, default=384)
     ap.add_argument("--reference-benchmark", action="store_true",
                     help="print only the reference's cylinder benchmark (compact and dense layouts)")
+    ap.add_argument("--configs", action="store_true", help="print only the per-config rates (C1, C2, C4, C5)")
     ap.add_argument("--cylinder-size", type=float, default=8.0)
     ap.add_argument("--cylinder-steps", type=int, default=20)
     ap.add_argument("--porous-steps", type=int, default=2000)
@@ -387,6 +388,9 @@ def main():
         return run_porous(args, local)
     if args.reference_benchmark:
         print(json.dumps(cylinder_benchmark(local, args.cylinder_size, args.cylinder_steps)), flush=True)
+        return 0
+    if args.configs:
+        print(json.dumps(config_benchmarks(local)), flush=True)
         return 0
     n = args.n
     ncell = n ** 3
