@@ -24,12 +24,12 @@
 
 namespace lbm {
 
-// Warps per block and blocks per SM, measured on GB300: the D3Q19 AA even
-// step runs best with 8-warp blocks, two per SM (128 registers); every other
-// kind, and all of D3Q27, with 4-warp blocks, three per SM (at most 170
+// Warps per block and blocks per SM, measured on GB300: D3Q19 AA even and AB
+// steps run best with 8-warp blocks, two per SM (128 registers); the D3Q19 AA
+// odd step and all of D3Q27 with 4-warp blocks, three per SM (at most 170
 // registers).
 template <int Q, int KIND>
-constexpr int async_warps() { return (Q == 19 && KIND == K_AA_EVEN) ? 8 : 4; }
+constexpr int async_warps() { return (Q == 19 && KIND != K_AA_ODD) ? 8 : 4; }
 template <int Q, int KIND>
 constexpr int async_min_blocks() { return async_warps<Q, KIND>() == 8 ? 2 : 3; }
 constexpr int kAsyncStages = 2;
