@@ -1,6 +1,8 @@
-"""Checkpoint and restart through the logical populations: a state read out
-after t steps (any AA parity, either AB buffer) and loaded into a fresh handle
-continues bit for bit like the uninterrupted run."""
+"""Checkpoint and restart: a state read out after t steps and loaded into a
+fresh handle continues bit for bit like the uninterrupted run.  AA saves the
+logical populations (a fresh handle starts at even parity; the logical layout
+is parity-free); AB saves the raw buffer (for AB pull it holds post-collision
+values, which the logical readout would stream once more)."""
 import numpy as np
 import pytest
 
@@ -30,10 +32,11 @@ def test_restart_from_logical_state(gpu, pattern, arithmetic, storage, t_save):
         first.set_solid(solid)
         first.set_populations(f0)
         first.step(t_save)
-        saved = first.get_populations("logical")
+        layout = "logical" if pattern == "aa" else "raw"
+        saved = first.get_populations(layout)
     with Simulation(nx, ny, nz, **kw) as second:
         second.set_solid(solid)
-        second.set_populations(saved)
+        second.set_populations(saved, layout)
         second.step(9 - t_save)
         out = second.get_populations("logical")
     fluid = ~solid.astype(bool)
