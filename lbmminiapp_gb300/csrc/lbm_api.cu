@@ -733,7 +733,8 @@ static lbm_status check_range(lbm_handle* h, int64_t start, int64_t count)
 
 lbm_status lbm_timestep_even_force(lbm_handle* h, void* dstrb, int64_t start, int64_t count)
 {
-   if (!h || !dstrb) return LBM_ERR_INVALID_ARGUMENT;
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (!dstrb) return fail(h, LBM_ERR_INVALID_ARGUMENT, "null population buffer");
    if (h->cfg.prop_pattern != LBM_PATTERN_AA) return fail(h, LBM_ERR_STATE, "handle is not configured for AA");
    lbm_status st = check_range(h, start, count);
    if (st != LBM_OK) return st;
@@ -743,7 +744,8 @@ lbm_status lbm_timestep_even_force(lbm_handle* h, void* dstrb, int64_t start, in
 
 lbm_status lbm_timestep_odd_force(lbm_handle* h, void* dstrb, int64_t start, int64_t count)
 {
-   if (!h || !dstrb) return LBM_ERR_INVALID_ARGUMENT;
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (!dstrb) return fail(h, LBM_ERR_INVALID_ARGUMENT, "null population buffer");
    if (h->cfg.prop_pattern != LBM_PATTERN_AA) return fail(h, LBM_ERR_STATE, "handle is not configured for AA");
    lbm_status st = check_range(h, start, count);
    if (st != LBM_OK) return st;
@@ -753,8 +755,10 @@ lbm_status lbm_timestep_odd_force(lbm_handle* h, void* dstrb, int64_t start, int
 
 lbm_status lbm_timestep_force(lbm_handle* h, const void* src, void* tgt, int64_t start, int64_t count)
 {
-   if (!h || !src || !tgt || src == tgt) return LBM_ERR_INVALID_ARGUMENT;
+   if (!h) return LBM_ERR_INVALID_ARGUMENT;
    if (h->cfg.prop_pattern != LBM_PATTERN_AB) return fail(h, LBM_ERR_STATE, "handle is not configured for AB");
+   if (!src || !tgt) return fail(h, LBM_ERR_INVALID_ARGUMENT, "null population buffer");
+   if (src == tgt) return fail(h, LBM_ERR_INVALID_ARGUMENT, "AB needs two distinct buffers");
    lbm_status st = check_range(h, start, count);
    if (st != LBM_OK) return st;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));

@@ -45,7 +45,7 @@ def test_bad_calls_give_status_codes(gpu):
             sim.timestep_even_force(buf, 0, sim.ncell + 1)
         assert e.value.status == 1
         with pytest.raises(LBMError) as e:
-            sim.timestep_force(buf, buf, 0, 10)      # AB call on an AA handle
+            sim.timestep_force(buf, buf + 8, 0, 10)      # AB call on an AA handle
         assert e.value.status == 6
         with pytest.raises(LBMError) as e:
             sim.set_porosity(np.full((6, 8, 12), 1.5))
