@@ -150,7 +150,7 @@ KParams make_params(const lbm_handle* h, int64_t start, int64_t end, Launch& L)
    L.pair_block = dim3(pbx, 1, 1);
    L.pair_grid = dim3((half + pbx - 1) / pbx, c.ny, (unsigned)(z1 - z0));
    L.async = h->storage == ST_F64 && h->arith == AR_F64X && start == 0 && end == h->ncell && L.idx32;
-   L.async_low = h->storage != ST_F64 && start == 0 && end == h->ncell && L.idx32;
+   L.async_low = h->storage != ST_F64 && start == 0 && end == h->ncell && (uint64_t)h->Q * (uint64_t)h->plane < (1ull << 32);
    L.ag = async_geom(c.nx, c.ny, c.nz);
    return p;
 }

@@ -34,11 +34,14 @@ __device__ __forceinline__ void cp_async4(uint32_t smem, const void* g)
    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem), "l"(g) : "memory");
 }
 
-// Direction-plane base pointers in the parameter bank (see PlanePtrs).
+// Buffers addressed by 32-bit element index slot * plane + cell (the launch
+// requires Q * plane < 2^32): a bounced-back direction only changes the
+// index, not the base pointer, so no per-direction pointer is selected.
 template <typename T>
 struct PlanePtrsT {
-   const T* src[27];
-   T* dst[27];
+   const T* src;
+   T* dst;
+   uint32_t plane;
 };
 
 // Raw stored value (S (f - w), as a float) from the copied word.
@@ -68,7 +71,7 @@ __device__ __forceinline__ uint32_t async_issue_low(const PlanePtrsT<typename St
    for (int s = 0; s < Q; s++) {
       const Access a = read_access<Q, KIND, LINKS>(tl.ci, tl.lk, s);
       const uint32_t e = c + (uint32_t)a.off;
-      const T* elem = pp.src[a.slot] + e;
+      const T* elem = pp.src + ((uint32_t)a.slot * pp.plane + e);
       const void* word = elem;
       if constexpr (sizeof(T) == 2) {
          word = reinterpret_cast<const void*>(reinterpret_cast<uintptr_t>(elem) & ~(uintptr_t)3);
@@ -120,7 +123,7 @@ __global__ void __launch_bounds__(kAsyncLowWarps * 32) step_async_low_kernel(
 #pragma unroll
          for (int s = 0; s < Q; s++) {
             const Access a = write_access<Q, KIND, LINKS>(cur.ci, cur.lk, s);
-            store_raw(pp.dst[a.slot] + (c + (uint32_t)a.off), o[s]);
+            store_raw(pp.dst + ((uint32_t)a.slot * pp.plane + c + (uint32_t)a.off), o[s]);
          }
       }
       if (next >= ag.ntiles) break;
@@ -159,12 +162,11 @@ cudaError_t launch_async_low(const KParams& p, const AsyncGeom& ag, const void* 
    }
    const uint32_t need = (ag.ntiles + kAsyncLowWarps - 1) / kAsyncLowWarps;
    const unsigned grid = (unsigned)(need < (uint32_t)cached ? need : (uint32_t)cached);
+   if ((uint64_t)Q * (uint64_t)p.plane >= (1ull << 32)) return cudaErrorInvalidValue;
    PlanePtrsT<T> pp;
-   for (int s = 0; s < 27; s++) {
-      const int k = s < Q ? s : 0;
-      pp.src[s] = static_cast<const T*>(src) + (int64_t)k * p.plane;
-      pp.dst[s] = static_cast<T*>(dst) + (int64_t)k * p.plane;
-   }
+   pp.src = static_cast<const T*>(src);
+   pp.dst = static_cast<T*>(dst);
+   pp.plane = (uint32_t)p.plane;
    kern<<<grid, kAsyncLowWarps * 32, smem, stream>>>(p, ag, pp);
    return cudaGetLastError();
 }
