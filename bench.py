@@ -66,7 +66,8 @@ def parse():
     ap.add_argument("--porous-n", type=int, default=384)
     ap.add_argument("--reference-benchmark", action="store_true",
                     help="print only the reference's cylinder benchmark (compact and dense layouts)")
-    ap.add_argument("--configs", action="store_true", help="print only the per-config rates (C1, C2, C4, C5)")
+    ap.add_argument("--configs", action="store_true",
+                    help="print only the rates of the other workloads (small box, channel, porous channel, spheres)")
     ap.add_argument("--cylinder-size", type=float, default=8.0)
     ap.add_argument("--cylinder-steps", type=int, default=20)
     ap.add_argument("--porous-steps", type=int, default=2000)
@@ -222,12 +223,12 @@ def traffic_per_launch():
 
 
 def config_benchmarks(device, steps=20):
-    """MLUPS (fluid cells) of the other configurations' shapes, each timed
-    over `steps` steps after 2 warm-up steps with CUDA events:
-    C1 D3Q19 AA FP64 64^3 periodic Taylor-Green (tau 0.8);
-    C2 D3Q27 AB push / pull FP64 256x128x128 channel, gx 1e-6 (tau 0.6);
-    C4 D3Q19 AA FP32 128x64x64 channel with the smoothed porosity field, gx 1e-5 (tau 0.7);
-    C5 D3Q27 AA FP16 384^3 sphere packing (solid fraction 0.35), gx 1e-6 (tau 0.7)."""
+    """MLUPS (fluid cells) of the other workloads' shapes, each timed over
+    `steps` steps after 2 warm-up steps with CUDA events:
+    D3Q19 AA FP64 64^3 periodic Taylor-Green (tau 0.8);
+    D3Q27 AB push / pull FP64 256x128x128 channel, gx 1e-6 (tau 0.6);
+    D3Q19 AA FP32 128x64x64 channel with the smoothed porosity field, gx 1e-5 (tau 0.7);
+    D3Q27 AA FP16 384^3 sphere packing (solid fraction 0.35), gx 1e-6 (tau 0.7)."""
     import torch
     import lbmminiapp_gb300 as lbm
     from lbmminiapp_gb300 import workloads
@@ -246,27 +247,27 @@ def config_benchmarks(device, steps=20):
     u = workloads.taylor_green(64, 64, 64, 0.05)
     with lbm.Simulation(64, 64, 64, lattice=19, pattern="aa", omega=1 / 0.8, force=(0, 0, 0), device=device) as sim:
         sim.init_equilibrium(None, u)
-        out["C1 q19 aa f64x 64^3"] = timed(sim, 200)
+        out["q19 aa f64x 64^3 periodic"] = timed(sim, 200)
     solid = workloads.channel_mask(256, 128, 128)
     for pattern in ("ab_push", "ab_pull"):
         with lbm.Simulation(256, 128, 128, lattice=27, pattern=pattern, omega=1 / 0.6, force=(1e-6, 0, 0),
                             periodic=(1, 0, 1), device=device) as sim:
             sim.set_solid(solid)
             sim.init_equilibrium()
-            out[f"C2 q27 {pattern} f64x 256x128x128 channel"] = timed(sim, steps)
+            out[f"q27 {pattern} f64x 256x128x128 channel"] = timed(sim, steps)
     solid = workloads.channel_mask(128, 64, 64)
     with lbm.Simulation(128, 64, 64, lattice=19, pattern="aa", omega=1 / 0.7, force=(1e-5, 0, 0), periodic=(1, 0, 1),
                         storage="f32", device=device) as sim:
         sim.set_solid(solid)
         sim.set_porosity(workloads.smoothed_porosity((64, 64, 128), sigma=3.0, seed=7))
         sim.init_equilibrium()
-        out["C4 q19 aa f32 128x64x64 channel + porosity"] = timed(sim, 100)
+        out["q19 aa f32 128x64x64 channel + porosity"] = timed(sim, 100)
     solid, _, _ = workloads.sphere_packing(384, 0.35, 6.0, 12.0, seed=2024)
     with lbm.Simulation(384, 384, 384, lattice=27, pattern="aa", omega=1 / 0.7, force=(1e-6, 0, 0), storage="f16",
                         device=device) as sim:
         sim.set_solid(solid)
         sim.init_equilibrium()
-        out["C5 q27 aa f16 384^3 spheres"] = timed(sim, steps)
+        out["q27 aa f16 384^3 spheres"] = timed(sim, steps)
     return out
 
 

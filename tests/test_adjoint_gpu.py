@@ -2,7 +2,7 @@
 differences.
 
 Gradient error: max_i |g_adj(i) - g_fd(i)| / max_i |g_fd(i)| over the probed
-cells.  Small cases: <= 1e-6.  Config C4 (128 x 64 x 64 channel, D3Q19,
+cells.  Small cases: <= 1e-6.  The porous channel (128 x 64 x 64, D3Q19,
 tau = 0.7, porosity from Gaussian noise smoothed with sigma = 3 and clipped,
 per-cell force g_x = 1e-5, 500 steps, loss = mean u_x on the plane x = Nx-1 over
 steps 451-500, checkpoint every 50, eps = 1e-4 at 16 seeded fluid cells):
@@ -120,7 +120,7 @@ def test_c4_channel_porosity_adjoint(gpu, storage):
     adj_s = np.array([gS[c] for c in cells])
     adj_f = np.array([gFx[c] for c in cells])
     es, ef = grad_err(adj_s, fd_s), grad_err(adj_f, fd_f)
-    print(f"C4 {storage}: loss {loss:.6e} grad err porosity {es:.2e} force {ef:.2e}")
+    print(f"porous channel {storage}: loss {loss:.6e} grad err porosity {es:.2e} force {ef:.2e}")
     assert loss > 0
     if storage == "f64":
         assert es < 1e-4 and ef < 1e-4
