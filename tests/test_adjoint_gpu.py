@@ -104,7 +104,7 @@ def test_autograd_function_matches_run_backward(gpu):
 
 
 @pytest.mark.parametrize("storage", ["f64", "f32"])
-def test_c4_channel_porosity_adjoint(gpu, storage):
+def test_porous_channel_adjoint(gpu, storage):
     nx, ny, nz = 128, 64, 64
     r, solid, poro, force = make_case(19, nx, ny, nz, 0.7, 500, 50, "velocity", (451, 500), storage=storage,
                                       seed=42)
