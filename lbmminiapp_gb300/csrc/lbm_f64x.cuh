@@ -420,8 +420,10 @@ __host__ __device__ constexpr int pair_dir(int Q, int p)
 constexpr uint32_t kHiQuarter = (uint32_t)(1023 - 2) << 20;   // 0.25
 
 // The fast-path collision on one cell.  bits[] holds the Q input patterns in
-// direction order and receives the Q output patterns.  Returns false (leaving
-// bits[] untouched) when the cell must take the exact path:
+// direction order; each output pattern is handed to emit(s, pattern).
+// Returns false when the cell must take the exact path (nothing is emitted
+// when an input check fails; after an output check fails every output has
+// been emitted, possibly wrong):
 //   * inputs: rest population in [0.25, 1), the others in [2^-32, 0.25), and
 //     rho < 2;
 //   * |3 v_d| < 0.3: |c.u| stays well below 1 - uu/2, so the pair sums
@@ -429,9 +431,23 @@ constexpr uint32_t kHiQuarter = (uint32_t)(1023 - 2) << 20;   // 0.25
 //   * outputs inside [2^-75, 1).
 // Work is organised by opposite pairs (s, opp(s)): cu, the quadratic term and
 // the omega*w*rho products are shared, since cu(opp) = -cu(s).
-template <int Q, bool FORCE>
-__host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], const x64::Consts& k,
-                                                          int compat)
+template <int Q, class Again>
+__host__ __device__ __forceinline__ x64::df input_pair(const x64::df (&f)[Q], const Again& again, int s)
+{
+   if constexpr (Again::kRefetch) return again(s);
+   else return f[s];
+}
+
+// Input policy of the fast path that splits the inputs once and keeps the
+// pairs in registers.
+struct KeepInputs {
+   static constexpr bool kRefetch = false;
+   __host__ __device__ __forceinline__ x64::df operator()(int) const { return {0.f, 0.f}; }
+};
+
+template <int Q, bool FORCE, class Emit, class Again>
+__host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (&bits)[Q], const x64::Consts& k,
+                                                               int compat, Emit& emit, const Again& again)
 {
    using namespace x64;
    constexpr int R = lat_rest(Q);
@@ -447,9 +463,13 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
    const uint32_t hr = (uint32_t)(bits[R] >> 32);
    if (hmin < kHiMin || hmax >= kHiQuarter || hr < kHiQuarter || hr >= kHiMax) return false;
 
+   // Float pairs of the inputs for the update's (1 - omega) f term: split
+   // here and kept, or made again from a second read of the inputs.
    df f[Q];
+   if constexpr (!Again::kRefetch) {
 #pragma unroll
-   for (int s = 0; s < Q; s++) f[s] = split(bits[s]);
+      for (int s = 0; s < Q; s++) f[s] = split(bits[s]);
+   }
 
    // rho and j = sum c_s f_s from the exact sums of the fixed-point images
    // floor(f * 2^53); rho < 2 is checked (rho's top word below 2^22).
@@ -517,15 +537,14 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
 #pragma unroll
    for (int cls = 0; cls < 4; cls++) owr[cls] = df_mul_u(k.ow[cls], rho);
 
-   // Results are written back only after every output passed its check (a
-   // fallback must still see the original inputs).
-   uint64_t res[Q - 1];
-   uint64_t rest_bits;
+   // Each output goes to emit(s, pattern) as soon as it is made; the return
+   // value says whether all of them passed the range check (if not, the
+   // caller overwrites every one with the exact result).
    JoinRange range;
    // rest direction: P = base
    {
       const df A = df_mul_u(owr[0], base);
-      const df a = df_mul_u(k.om1, f[R]);
+      const df a = df_mul_u(k.om1, input_pair(f, again, R));
       const df t = two_sum(A.h, a.h);
       df out = {t.h, fadd(t.l, fadd(A.l, a.l))};
       if (FORCE) {
@@ -534,7 +553,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
          const df t2 = two_sum(out.h, -fr.h);
          out = {t2.h, fadd(t2.l, fsub(out.l, fr.l))};
       }
-      rest_bits = join(out, range);
+      emit(R, join(out, range));
    }
 #pragma unroll
    for (int q = 0; q < NP; q++) {
@@ -573,7 +592,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
       // s: A + B ; opp(s): A - B ; then + (1 - omega) f
       {
          const df tp = fast_two_sum(A.h, B.h);
-         const df a = df_mul_u(k.om1, f[s]);
+         const df a = df_mul_u(k.om1, input_pair(f, again, s));
          const df t = two_sum(tp.h, a.h);
          df out = {t.h, fadd(t.l, fadd(tp.l, fadd(fadd(A.l, B.l), a.l)))};
          if (FORCE) {
@@ -581,11 +600,11 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
             const df t2 = two_sum(out.h, fr.h);
             out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fadd(k.Kf[s].l, sym.l))))};
          }
-         res[q] = join(out, range);
+         emit(s, join(out, range));
       }
       {
          const df tm = fast_two_sum(A.h, -B.h);
-         const df a = df_mul_u(k.om1, f[o]);
+         const df a = df_mul_u(k.om1, input_pair(f, again, o));
          const df t = two_sum(tm.h, a.h);
          df out = {t.h, fadd(t.l, fadd(tm.l, fadd(fsub(A.l, B.l), a.l)))};
          if (FORCE) {
@@ -593,17 +612,30 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], 
             const df t2 = two_sum(out.h, fr.h);
             out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fsub(sym.l, k.Kf[s].l))))};
          }
-         res[NP + q] = join(out, range);
+         emit(o, join(out, range));
       }
    }
-   if (!range.ok()) return false;
+   return range.ok();
+}
+
+// Emitter that collects the outputs in registers.
+template <int Q>
+struct EmitToArray {
+   uint64_t res[Q];
+   __host__ __device__ __forceinline__ void operator()(int s, uint64_t v) { res[s] = v; }
+};
+
+
+// The fast path on bits[] in place: returns false, leaving bits[] untouched,
+// when the cell must take the exact path.
+template <int Q, bool FORCE>
+__host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], const x64::Consts& k,
+                                                          int compat)
+{
+   EmitToArray<Q> out;
+   if (!collide_f64x_fast_emit<Q, FORCE>(bits, k, compat, out, KeepInputs{})) return false;
 #pragma unroll
-   for (int q = 0; q < NP; q++) {
-      const int s = pair_dir(Q, q);
-      bits[s] = res[q];
-      bits[lat_opp(Q, s)] = res[NP + q];
-   }
-   bits[R] = rest_bits;
+   for (int s = 0; s < Q; s++) bits[s] = out.res[s];
    return true;
 }
 
@@ -653,9 +685,10 @@ __device__ __forceinline__ void collide_f64x(uint64_t (&bits)[Q], const KParams&
    collide_exact_bits<Q>(bits, p);
 }
 
-// The same for inputs that stay in shared memory (direction s at
-// in[32 s]): the fallback reads them again from there, so the input
-// patterns need not stay in registers through the fast path.
+// The same for inputs that stay in shared memory (direction s at in[32 s]),
+// with the outputs left in bits[]: the fallback reads the inputs again from
+// there, so the input patterns need not stay in registers through the fast
+// path.
 template <int Q>
 __device__ __forceinline__ void collide_f64x_shared(const unsigned long long* in, uint64_t (&bits)[Q],
                                                     const KParams& p)
@@ -674,6 +707,47 @@ __device__ __forceinline__ void collide_f64x_shared(const unsigned long long* in
       bits[s] = v;
    }
    collide_exact_bits<Q>(bits, p);
+}
+
+// Input pattern s read again from shared memory (direction s at byte 256 s
+// from the lane's first), raw or split into a float pair.  The load is
+// volatile so that the compiler does not keep the first load's value live in
+// registers instead.
+struct AgainFromShared {
+   static constexpr bool kRefetch = true;
+   uint32_t addr;
+   __device__ __forceinline__ uint64_t raw(int s) const
+   {
+      unsigned long long v;
+      asm volatile("ld.shared.u64 %0, [%1];\n" : "=l"(v) : "r"(addr + 256u * (uint32_t)s));
+      return v;
+   }
+   __device__ __forceinline__ x64::df operator()(int s) const { return x64::split(raw(s)); }
+};
+
+// The same again, with each output handed to emit(s, pattern) as it is made, so neither the
+// input nor the output patterns stay in registers through the fast path: the
+// moment sums read the inputs once, the update reads them again.  If
+// the fast path fails after emitting, the exact results are emitted again
+// over them (the fallback reads its inputs from shared memory): a caller's
+// emit must let a later emit of the same s win, as stores from one thread to
+// one address do.
+template <int Q, class Emit>
+__device__ __forceinline__ void collide_f64x_shared_emit(const unsigned long long* in, const KParams& p, Emit& emit)
+{
+   uint64_t bits[Q];
+#pragma unroll
+   for (int s = 0; s < Q; s++) bits[s] = in[s * 32];
+   const x64::Consts k = collide_consts<Q>(p);
+   const AgainFromShared again{(uint32_t)__cvta_generic_to_shared(in)};
+   const bool fast = p.forced ? collide_f64x_fast_emit<Q, true>(bits, k, p.compat, emit, again)
+                              : collide_f64x_fast_emit<Q, false>(bits, k, p.compat, emit, again);
+   if (fast) return;
+#pragma unroll
+   for (int s = 0; s < Q; s++) bits[s] = again.raw(s);
+   collide_exact_bits<Q>(bits, p);
+#pragma unroll
+   for (int s = 0; s < Q; s++) emit(s, bits[s]);
 }
 
 }  // namespace lbm

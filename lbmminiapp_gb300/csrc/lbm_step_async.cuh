@@ -24,15 +24,22 @@
 
 namespace lbm {
 
-// Warps per block and blocks per SM, measured on GB300: D3Q19 AA even and AB
-// steps run best with 8-warp blocks, two per SM (128 registers); the D3Q19 AA
-// odd step and all of D3Q27 with 4-warp blocks, three per SM (at most 170
-// registers).
+// Warps per block and blocks per SM, measured on GB300: D3Q19 steps run best
+// with 8-warp blocks, two per SM (128 registers), D3Q27 steps with 4-warp
+// blocks, three per SM (at most 170 registers; at 128 they spill and run
+// 15-20 % slower).
 template <int Q, int KIND>
-constexpr int async_warps() { return (Q == 19 && KIND != K_AA_ODD) ? 8 : 4; }
+constexpr int async_warps() { return Q == 19 ? 8 : 4; }
 template <int Q, int KIND>
 constexpr int async_min_blocks() { return async_warps<Q, KIND>() == 8 ? 2 : 3; }
 constexpr int kAsyncStages = 2;
+// Whether a step stores each output as the collision makes it (and re-reads
+// its inputs from shared memory for the update), which frees the registers
+// of Q input and Q output patterns; measured faster for every kind but the
+// D3Q27 AB steps, which keep their outputs in registers and store them after
+// the collision.
+template <int Q, int KIND>
+constexpr bool async_stream_out() { return !(Q == 27 && (KIND == K_AB_PUSH || KIND == K_AB_PULL)); }
 
 template <int Q, int KIND>
 constexpr size_t async_smem_bytes()
@@ -130,6 +137,21 @@ __device__ __forceinline__ void async_issue(const PlanePtrs& pp, const TileLane&
    }
 }
 
+// Stores each output straight to its target slot.  AA stays race-free with
+// stores that may be overwritten later by the same thread (the fast path's
+// outputs when a range check fails): the locations are this cell's own.
+template <int Q, int KIND, bool LINKS>
+struct StoreEmit {
+   const PlanePtrs& pp;
+   const CellIndex& ci;
+   uint32_t lk;
+   __device__ __forceinline__ void operator()(int s, uint64_t v) const
+   {
+      const Access a = write_access<Q, KIND, LINKS>(ci, lk, s);
+      pp.dst[a.slot][(uint32_t)ci.c + (uint32_t)a.off] = v;
+   }
+};
+
 template <int Q, int KIND, bool LINKS, bool RAGGED>
 __global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<Q, KIND>()) step_async_kernel(const KParams p, const AsyncGeom ag,
                                                                       const PlanePtrs pp)
@@ -161,13 +183,14 @@ __global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<
       cp_async_commit();
       cp_async_wait_prev();
       if (!(LINKS || RAGGED) || cur.active) {
-         uint64_t bits[Q];
-         collide_f64x_shared<Q>(mine + stage * Q * 32 + lane, bits, p);
-         const uint32_t c = (uint32_t)cur.ci.c;
+         StoreEmit<Q, KIND, LINKS> emit{pp, cur.ci, cur.lk};
+         if constexpr (async_stream_out<Q, KIND>()) {
+            collide_f64x_shared_emit<Q>(mine + stage * Q * 32 + lane, p, emit);
+         } else {
+            uint64_t bits[Q];
+            collide_f64x_shared<Q>(mine + stage * Q * 32 + lane, bits, p);
 #pragma unroll
-         for (int s = 0; s < Q; s++) {
-            const Access a = write_access<Q, KIND, LINKS>(cur.ci, cur.lk, s);
-            pp.dst[a.slot][c + (uint32_t)a.off] = bits[s];
+            for (int s = 0; s < Q; s++) emit(s, bits[s]);
          }
       }
       if (next >= ag.ntiles) break;
