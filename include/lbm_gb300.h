@@ -151,8 +151,11 @@ lbm_status lbm_step(lbm_handle* h, int nsteps);
  * PropagationAB.cpp:222-281). */
 lbm_status lbm_get_macros(lbm_handle* h, double* rho, double* u);
 /* FP64 sums over fluid cells of rho and rho*u (no F/2 shift) from the logical
- * populations: out[0]=mass, out[1..3]=momentum.  LBM_ERR_DIVERGED when a sum is
- * not finite.  No reference counterpart. */
+ * populations: out[0]=mass, out[1..3]=momentum.  Cells whose populations all
+ * lie in [2^-32, 1) are summed exactly (128-bit fixed point) and the totals
+ * rounded once, so they do not depend on launch shapes; other cells are
+ * summed in FP64.  LBM_ERR_DIVERGED when a sum is not finite.  No reference
+ * counterpart. */
 lbm_status lbm_reduce_conserved(lbm_handle* h, double out[4]);
 
 /* ---- kernel-level entry points on caller-owned device buffers.
@@ -251,7 +254,7 @@ lbm_status lbm_sparse_timestep_force(lbm_sparse_handle* h, const double* src, do
  * pull).  Asynchronous on `stream` (cudaStream_t as void*, NULL = legacy
  * default stream), on the current device; out is not checked for NaN/Inf.
  * Calls no cudaMalloc: the per-block partial sums live in a static device
- * array of 512 KiB that every GPU loading the library keeps until exit, so at
+ * array of 384 KiB that every GPU loading the library keeps until exit, so at
  * most 2^28 (268,435,456) cells are accepted; larger grids return
  * LBM_ERR_INVALID_ARGUMENT.  The first call on each device looks the array's
  * address up (cudaGetSymbolAddress) with that device current; make that first

@@ -40,7 +40,7 @@ struct lbm_handle {
    cudaStream_t copy_stream = nullptr;   // host <-> staging copies of the chunked transfers
    cudaEvent_t chunk_ready[2] = {nullptr, nullptr};
    cudaEvent_t chunk_free[2] = {nullptr, nullptr};
-   double* partials = nullptr;     // reduction scratch: kReduceBlocks * 4 doubles
+   double* partials = nullptr;     // reduction scratch: plane partials or 4 doubles per loss block
    double* reduce_out = nullptr;   // 4 doubles
    cudaStream_t stream = nullptr;
    std::string err;
@@ -217,8 +217,9 @@ template <int Q, int ST>
 struct ExportPlane {
    static void run(const lbm_handle* h, const void* buf, int s, int mode)
    {
-      export_plane_kernel<Q, ST><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(dims_of(h), buf, h->links, s,
-                                                                                    mode, h->staging);
+      export_plane_kernel<Q, ST><<<blocks_for(h->ncell, 256), 256, 0, h->stream>>>(dims_of(h), buf, h->links,
+                                                                                    plane_dir(Q, s), mode,
+                                                                                    h->staging);
    }
 };
 
@@ -236,9 +237,12 @@ template <int Q, int ST>
 struct Conserved {
    static void run(const lbm_handle* h, const void* buf, int mode, double* partials, double* out)
    {
-      conserved_partial_kernel<Q, ST><<<kReduceBlocks, kReduceThreads, 0, h->stream>>>(dims_of(h), buf, h->links,
-                                                                                         mode, partials);
-      conserved_final_kernel<<<1, kReduceThreads, 0, h->stream>>>(partials, kReduceBlocks, out);
+      PlanePartial* part = reinterpret_cast<PlanePartial*>(partials);
+      const int64_t per_range = plane_per_range(h->ncell);
+      const int nblocks = plane_blocks(Q, h->ncell);
+      conserved_plane_kernel<Q, ST><<<nblocks, kReduceThreads, 0, h->stream>>>(dims_of(h), buf, h->links, mode,
+                                                                              per_range, part);
+      conserved_plane_final_kernel<Q><<<1, kReduceThreads, 0, h->stream>>>(part, nblocks, mode, out);
    }
 };
 
@@ -389,7 +393,12 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_handle** out)
    if (st == LBM_OK && c.prop_pattern == LBM_PATTERN_AB) st = dev_alloc(h, &h->buf[1], h->buffer_bytes);
    h->staging_elems = std::max<size_t>((size_t)h->ncell, kMinStaging);
    if (st == LBM_OK) st = dev_alloc(h, (void**)&h->staging, sizeof(double) * h->staging_elems);
-   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->partials, sizeof(double) * 4 * kReduceBlocks);
+   if (st == LBM_OK) {
+      // the plane reduction's partials, or the loss reduction's 4 doubles per block
+      const size_t plane_bytes = sizeof(PlanePartial) * (size_t)27 * kPlaneRanges;
+      const size_t loss_bytes = sizeof(double) * 4 * kReduceBlocks;
+      st = dev_alloc(h, (void**)&h->partials, plane_bytes > loss_bytes ? plane_bytes : loss_bytes);
+   }
    if (st == LBM_OK) st = dev_alloc(h, (void**)&h->reduce_out, sizeof(double) * 4);
    if (st == LBM_OK) st = lbm_set_solid(h, nullptr);
    if (st == LBM_OK) st = lbm_init_equilibrium(h, nullptr, nullptr);

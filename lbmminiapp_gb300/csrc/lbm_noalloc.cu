@@ -8,13 +8,16 @@
 // as caller-owned device memory and keeps its only scratch -- one FP64 partial
 // sum per block -- in a file-scope device array instead of an allocation.
 //
-// The scratch array holds kNoAllocMaxBlocks partials (4 doubles each, 512 KiB)
-// and lives on every GPU that loads the library until the process exits.  One
-// block reduces kNoAllocCellsPerBlock consecutive cells, so the entry point
-// accepts at most kNoAllocMaxBlocks * kNoAllocCellsPerBlock = 2^28 cells and
-// rejects larger grids.  Every call shares the array; each launch writes every
-// partial its final pass reads, so nothing needs clearing, but two calls that
-// overlap on the GPU (different streams, no ordering) race on it.
+// The sums are the handle reduction's (exact 128-bit fixed-point sums for
+// cells whose populations lie in [2^-32, 1), FP64 for the others).  The
+// scratch array holds kNoAllocMaxBlocks partials (96 bytes each, 384 KiB)
+// and lives on every GPU that loads the library until the process exits.
+// One block reduces a run of consecutive cells, at least kNoAllocMinCells
+// and as many as keep the block count within kNoAllocMaxBlocks; the entry
+// point accepts at most 2^28 cells and rejects larger grids.  Every call
+// shares the array; each launch writes every partial its final pass reads, so
+// nothing needs clearing, but two calls that overlap on the GPU (different
+// streams, no ordering) race on it.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -28,15 +31,16 @@ using namespace lbm;
 namespace {
 
 constexpr int kNoAllocThreads = 256;
-constexpr int kNoAllocMaxBlocks = 16384;
-constexpr int64_t kNoAllocCellsPerBlock = 16384;
+constexpr int kNoAllocMaxBlocks = 4096;
+constexpr int64_t kNoAllocMinCells = 4096;
+constexpr int64_t kNoAllocMaxCells = (int64_t)1 << 28;
 constexpr int kNoAllocMaxDevices = 64;
 
-static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxBlocks * 4];
+static __device__ __align__(256) ConservedPartial g_noalloc_partials[kNoAllocMaxBlocks];
 
 // Device address of g_noalloc_partials per device ordinal, looked up once per
 // device with that device current (host code must not use the symbol itself).
-double* g_scratch_addr[kNoAllocMaxDevices] = {};
+ConservedPartial* g_scratch_addr[kNoAllocMaxDevices] = {};
 std::mutex g_scratch_mutex;
 
 // Direction s of cell (x, y, z) with the slot convention `mode` (0: slot s,
@@ -54,49 +58,34 @@ __device__ __forceinline__ double logical_pop_mask(const GridDims& g, const void
    return load_pop<ST>(buf, (int64_t)s * g.plane + n, lat_w(Q, s));
 }
 
+// Block b reduces the cells [b * per_block, (b + 1) * per_block).
 template <int Q, int ST>
 __global__ void __launch_bounds__(kNoAllocThreads) conserved_chunk_kernel(GridDims g, const void* buf,
                                                                           const uint8_t* solid, int mode,
-                                                                          double* partials)
+                                                                          int64_t per_block,
+                                                                          ConservedPartial* partials)
 {
-   double acc[4] = {0.0, 0.0, 0.0, 0.0};
-   const int64_t begin = (int64_t)blockIdx.x * kNoAllocCellsPerBlock;
-   const int64_t end = begin + kNoAllocCellsPerBlock < g.ncell ? begin + kNoAllocCellsPerBlock : g.ncell;
+   ConservedAcc acc;
+   conserved_zero(acc);
+   const int64_t begin = (int64_t)blockIdx.x * per_block;
+   const int64_t end = begin + per_block < g.ncell ? begin + per_block : g.ncell;
    for (int64_t c = begin + threadIdx.x; c < end; c += blockDim.x) {
       if (solid && solid[c]) continue;
       int x, y, z;
       cell_xyz(g, c, x, y, z);
+      double f[Q];
 #pragma unroll
-      for (int s = 0; s < Q; s++) {
-         const double f = logical_pop_mask<Q, ST>(g, buf, solid, x, y, z, c, s, mode);
-         acc[0] += f;
-         acc[1] += f * lat_c(Q, s, 0);
-         acc[2] += f * lat_c(Q, s, 1);
-         acc[3] += f * lat_c(Q, s, 2);
-      }
+      for (int s = 0; s < Q; s++) f[s] = logical_pop_mask<Q, ST>(g, buf, solid, x, y, z, c, s, mode);
+      conserved_add_cell<Q>(f, acc);
    }
-   __shared__ double sh[4][kNoAllocThreads / 32];
-   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-   for (int k = 0; k < 4; k++) {
-      double v = acc[k];
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, off);
-      if (lane == 0) sh[k][warp] = v;
-   }
-   __syncthreads();
-   if (threadIdx.x < 4) {
-      double v = 0.0;
-      for (int w = 0; w < kNoAllocThreads / 32; w++) v += sh[threadIdx.x][w];
-      partials[(int64_t)blockIdx.x * 4 + threadIdx.x] = v;
-   }
+   conserved_block_store<kNoAllocThreads>(acc, partials + blockIdx.x);
 }
 
 template <int Q, int ST>
-cudaError_t launch_chunks(const GridDims& g, const void* buf, const uint8_t* solid, int mode, double* scratch,
-                          int nblocks, cudaStream_t st)
+cudaError_t launch_chunks(const GridDims& g, const void* buf, const uint8_t* solid, int mode,
+                          ConservedPartial* scratch, int64_t per_block, int nblocks, cudaStream_t st)
 {
-   conserved_chunk_kernel<Q, ST><<<nblocks, kNoAllocThreads, 0, st>>>(g, buf, solid, mode, scratch);
+   conserved_chunk_kernel<Q, ST><<<nblocks, kNoAllocThreads, 0, st>>>(g, buf, solid, mode, per_block, scratch);
    return cudaGetLastError();
 }
 
@@ -118,7 +107,7 @@ extern "C" lbm_status lbm_reduce_conserved_noalloc(int lattice, int storage, int
    if (nx < 1 || ny < 1 || nz < 1 || !dstrb || !out || !periodic || readout < 0 || readout > 2)
       return noalloc_fail(LBM_ERR_INVALID_ARGUMENT, "bad grid, pointer or readout mode");
    const int64_t ncell = (int64_t)nx * ny * nz;
-   if (ncell > (int64_t)kNoAllocMaxBlocks * kNoAllocCellsPerBlock)
+   if (ncell > kNoAllocMaxCells)
       return noalloc_fail(LBM_ERR_INVALID_ARGUMENT,
                           "grid exceeds the static scratch: at most 268435456 cells (2^28)");
    if (plane_stride < ncell) return noalloc_fail(LBM_ERR_INVALID_ARGUMENT, "plane_stride below nx*ny*nz");
@@ -127,7 +116,7 @@ extern "C" lbm_status lbm_reduce_conserved_noalloc(int lattice, int storage, int
    cudaError_t e = cudaGetDevice(&dev);
    if (e != cudaSuccess) return noalloc_fail(LBM_ERR_CUDA, cudaGetErrorString(e));
    if (dev < 0 || dev >= kNoAllocMaxDevices) return noalloc_fail(LBM_ERR_UNSUPPORTED, "device ordinal above 63");
-   double* scratch = nullptr;
+   ConservedPartial* scratch = nullptr;
    {
       std::lock_guard<std::mutex> lock(g_scratch_mutex);
       if (!g_scratch_addr[dev]) {
@@ -148,21 +137,26 @@ extern "C" lbm_status lbm_reduce_conserved_noalloc(int lattice, int storage, int
    g.ncell = ncell;
    g.plane = plane_stride;
    for (int d = 0; d < 3; d++) g.periodic[d] = periodic[d] ? 1 : 0;
-   const int nblocks = (int)((ncell + kNoAllocCellsPerBlock - 1) / kNoAllocCellsPerBlock);
+   // runs of at least kNoAllocMinCells cells, a multiple of the block size,
+   // in at most kNoAllocMaxBlocks blocks (2^28 / 4096 = 65536 cells at most)
+   int64_t per_block = (ncell + kNoAllocMaxBlocks - 1) / kNoAllocMaxBlocks;
+   per_block = per_block < kNoAllocMinCells ? kNoAllocMinCells : per_block;
+   per_block = (per_block + kNoAllocThreads - 1) / kNoAllocThreads * kNoAllocThreads;
+   const int nblocks = (int)((ncell + per_block - 1) / per_block);
    cudaStream_t st = static_cast<cudaStream_t>(stream);
    if (lattice == 19) {
       switch (storage) {
-         case LBM_STORE_F64: e = launch_chunks<19, ST_F64>(g, dstrb, solid, readout, scratch, nblocks, st); break;
-         case LBM_STORE_F32: e = launch_chunks<19, ST_F32>(g, dstrb, solid, readout, scratch, nblocks, st); break;
-         case LBM_STORE_BF16: e = launch_chunks<19, ST_BF16>(g, dstrb, solid, readout, scratch, nblocks, st); break;
-         default: e = launch_chunks<19, ST_F16>(g, dstrb, solid, readout, scratch, nblocks, st); break;
+         case LBM_STORE_F64: e = launch_chunks<19, ST_F64>(g, dstrb, solid, readout, scratch, per_block, nblocks, st); break;
+         case LBM_STORE_F32: e = launch_chunks<19, ST_F32>(g, dstrb, solid, readout, scratch, per_block, nblocks, st); break;
+         case LBM_STORE_BF16: e = launch_chunks<19, ST_BF16>(g, dstrb, solid, readout, scratch, per_block, nblocks, st); break;
+         default: e = launch_chunks<19, ST_F16>(g, dstrb, solid, readout, scratch, per_block, nblocks, st); break;
       }
    } else {
       switch (storage) {
-         case LBM_STORE_F64: e = launch_chunks<27, ST_F64>(g, dstrb, solid, readout, scratch, nblocks, st); break;
-         case LBM_STORE_F32: e = launch_chunks<27, ST_F32>(g, dstrb, solid, readout, scratch, nblocks, st); break;
-         case LBM_STORE_BF16: e = launch_chunks<27, ST_BF16>(g, dstrb, solid, readout, scratch, nblocks, st); break;
-         default: e = launch_chunks<27, ST_F16>(g, dstrb, solid, readout, scratch, nblocks, st); break;
+         case LBM_STORE_F64: e = launch_chunks<27, ST_F64>(g, dstrb, solid, readout, scratch, per_block, nblocks, st); break;
+         case LBM_STORE_F32: e = launch_chunks<27, ST_F32>(g, dstrb, solid, readout, scratch, per_block, nblocks, st); break;
+         case LBM_STORE_BF16: e = launch_chunks<27, ST_BF16>(g, dstrb, solid, readout, scratch, per_block, nblocks, st); break;
+         default: e = launch_chunks<27, ST_F16>(g, dstrb, solid, readout, scratch, per_block, nblocks, st); break;
       }
    }
    if (e != cudaSuccess) return noalloc_fail(LBM_ERR_CUDA, cudaGetErrorString(e));

@@ -18,7 +18,9 @@ from lbmminiapp_gb300 import _native as N
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-12  # relative; the two reductions add the same FP64 terms in different orders
+# Both reductions sum cells with populations in [2^-32, 1) exactly (128-bit
+# fixed point), so on these states they agree bit for bit although they split
+# the grid into blocks differently.
 
 
 def readout_mode(pattern, t):
@@ -61,8 +63,7 @@ def test_noalloc_matches_handle_reduction(gpu, Q, pattern, storage, walls, steps
             torch.cuda.synchronize()
             got = out.cpu().numpy()
             assert np.all(np.isfinite(got))
-            assert abs(got[0] - expected[0]) <= TOL * abs(expected[0])
-            assert np.all(np.abs(got[1:] - expected[1:]) <= TOL * abs(expected[0]))
+            assert np.array_equal(got, expected), (got, expected)
 
 
 def test_noalloc_rejects_grids_beyond_its_scratch(gpu):
