@@ -160,6 +160,16 @@ __host__ __device__ __forceinline__ float i2f_rn(int32_t i)
 #endif
 }
 
+// An integer-valued float (|x| < 2^31) to int32, exactly.
+__host__ __device__ __forceinline__ int32_t f2i_exact(float x)
+{
+#ifdef __CUDA_ARCH__
+   return __float2int_rz(x);
+#else
+   return (int32_t)x;
+#endif
+}
+
 __host__ __device__ __forceinline__ float u2f_rn(uint32_t u)
 {
 #ifdef __CUDA_ARCH__
@@ -274,14 +284,18 @@ __host__ __device__ __forceinline__ uint64_t fixed53(uint64_t bits)
    return ((uint64_t)(mh >> k) << 32) | funnel_r(lo, mh, k);
 }
 
-// Float pair of v * 2^-53 for a signed 64-bit v with |v| < 2^54: the top
-// part v >> 30 is an exact float, the low 30 bits are rounded to 24
-// (absolute error <= 2^-48).  Not normalised: h may be 0 or below l.
+// Float pair of v * 2^-53 for a signed 64-bit v with |v| < 2^54.  The top
+// part is v >> 23 rounded to 24 bits (an integer, so the remainder is exact
+// and below 2^30), the remainder is rounded to 24 bits: the pair is exact for
+// |v| < 2^47 and within 2^-48 |v| above, relative to v however small it is
+// (a momentum sum of a slow flow keeps every bit).  Not normalised: h may be
+// 0 or below l.
 __host__ __device__ __forceinline__ df fixed53_to_pair(int64_t v)
 {
    const uint32_t lo = (uint32_t)v, hi = (uint32_t)((uint64_t)v >> 32);
-   const int32_t top = (int32_t)funnel_l(lo, hi, 2);        // v >> 30 (arithmetic)
-   return {fmul(i2f_rn(top), 0x1p-23f), fmul(u2f_rn(lo & 0x3FFFFFFFu), 0x1p-53f)};
+   const float hf = i2f_rn((int32_t)funnel_l(lo, hi, 9));   // v >> 23 (arithmetic), rounded
+   const int32_t r = (int32_t)(lo - ((uint32_t)f2i_exact(hf) << 23));   // v - hf * 2^23, |r| < 2^30
+   return {fmul(hf, 0x1p-30f), fmul(i2f_rn(r), 0x1p-53f)};
 }
 
 // Non-negative float to unsigned int, rounded to nearest even.
@@ -365,6 +379,21 @@ struct Consts {
 
 // Host: the collision constants of a launch (relaxation rate, uniform force,
 // the Q19 AA Unroll rest-weight switch) in double, float and float-pair form.
+// Forcing form of the F64X fast path: 0 no force; 1 any force (the forcing
+// terms are added after the equilibrium with error-free sums); 2 a force small
+// enough, sum |F_d| <= 0.004 omega, for the terms to be folded into the
+// equilibrium's symmetric and antisymmetric parts.  The fast path's inputs
+// give rho >= 1/4, |3 v_d| < 0.3, hence omega w rho (Q+ - |3 c.v|) >=
+// 0.11 omega w, while the folded terms stay below 6.2 w sum |F_d|, so the
+// Fast2Sum operand order still holds (with a 4.5x margin at the bound).
+inline int force_mode(const double force[3], double omega)
+{
+   double fsum = 0.0;
+   for (int d = 0; d < 3; d++) fsum += force[d] < 0.0 ? -force[d] : force[d];
+   if (fsum == 0.0) return 0;
+   return fsum <= 0.004 * omega ? 2 : 1;
+}
+
 inline void set_collision_constants(KParams& p, int Q, double omega, const double force[3], int compat)
 {
    p.omega = omega;
@@ -399,7 +428,7 @@ inline void set_collision_constants(KParams& p, int Q, double omega, const doubl
    }
    for (int d = 0; d < 3; d++) split(3.0 * force[d], p.x_F3[d]);
    split(p.om2 / 36.0, p.x_om2w36);
-   p.forced = (force[0] != 0.0 || force[1] != 0.0 || force[2] != 0.0) ? 1 : 0;
+   p.forced = force_mode(force, omega);
 }
 
 // Representative s < opp(s) of the p-th opposite pair (direction order of
@@ -445,7 +474,7 @@ struct KeepInputs {
    __host__ __device__ __forceinline__ x64::df operator()(int) const { return {0.f, 0.f}; }
 };
 
-template <int Q, bool FORCE, class Emit, class Again>
+template <int Q, int FORCE, class Emit, class Again>
 __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (&bits)[Q], const x64::Consts& k,
                                                                int compat, Emit& emit, const Again& again)
 {
@@ -491,7 +520,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (
    df j[3];
 #pragma unroll
    for (int d = 0; d < 3; d++) {
-      // Fast2Sum is exact here: t.h is 0 or a multiple of 2^-23 above |t.l|.
+      // Fast2Sum is exact here: t.h is 0 or at least ulp-aligned above |t.l|.
       const df t = fixed53_to_pair(jx[d]);
       j[d] = fast_two_sum(t.h, t.l);
    }
@@ -543,11 +572,18 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (
    JoinRange range;
    // rest direction: P = base
    {
-      const df A = df_mul_u(owr[0], base);
+      df A = df_mul_u(owr[0], base);
+      if (FORCE == 2) {
+         // -(1 - omega/2) wf fu (wf = 1/36 with the Unroll-kernel weights),
+         // folded into the equilibrium term
+         const df fr = df_mul_u(compat ? k.om2w36 : k.om2w[0], fu);
+         const df t2 = fast_two_sum(A.h, -fr.h);
+         A = {t2.h, fadd(t2.l, fsub(A.l, fr.l))};
+      }
       const df a = df_mul_u(k.om1, input_pair(f, again, R));
       const df t = two_sum(A.h, a.h);
       df out = {t.h, fadd(t.l, fadd(A.l, a.l))};
-      if (FORCE) {
+      if (FORCE == 1) {
          // -(1 - omega/2) wf fu, wf = 1/36 with the Unroll-kernel weights
          const df fr = df_mul_u(compat ? k.om2w36 : k.om2w[0], fu);
          const df t2 = two_sum(out.h, -fr.h);
@@ -578,8 +614,8 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (
       const df c2h = df_sqr_u(cu);
       const df qs = fast_two_sum(base.h, 0.5f * c2h.h);
       const df Qp = {qs.h, fadd(qs.l, fadd(base.l, 0.5f * c2h.l))};
-      const df A = df_mul_u(owr[cls], Qp);   // omega * eq, symmetric part
-      const df B = df_mul_u(owr[cls], cu);   // omega * eq, antisymmetric part
+      df A = df_mul_u(owr[cls], Qp);   // omega * eq, symmetric part
+      df B = df_mul_u(owr[cls], cu);   // omega * eq, antisymmetric part
       // forcing om2 w (+-cf - fu + cu cf) = +-Kf[s] + (Kf[s] cu - om2 w fu), with
       // Kf[s] = om2 w cf a float pair made on the host
       df sym = {0.f, 0.f};
@@ -589,13 +625,21 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (
          const df t3 = two_sum(gc.h, -wf.h);
          sym = {t3.h, fadd(t3.l, fsub(gc.l, wf.l))};
       }
+      if (FORCE == 2) {
+         // small force: sym joins the symmetric part (far below it) and
+         // Kf[s] the antisymmetric part (which may vanish, hence TwoSum)
+         const df as = fast_two_sum(A.h, sym.h);
+         A = {as.h, fadd(as.l, fadd(A.l, sym.l))};
+         const df bs = two_sum(B.h, k.Kf[s].h);
+         B = {bs.h, fadd(bs.l, fadd(B.l, k.Kf[s].l))};
+      }
       // s: A + B ; opp(s): A - B ; then + (1 - omega) f
       {
          const df tp = fast_two_sum(A.h, B.h);
          const df a = df_mul_u(k.om1, input_pair(f, again, s));
          const df t = two_sum(tp.h, a.h);
          df out = {t.h, fadd(t.l, fadd(tp.l, fadd(fadd(A.l, B.l), a.l)))};
-         if (FORCE) {
+         if (FORCE == 1) {
             const df fr = two_sum(k.Kf[s].h, sym.h);
             const df t2 = two_sum(out.h, fr.h);
             out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fadd(k.Kf[s].l, sym.l))))};
@@ -607,7 +651,7 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (
          const df a = df_mul_u(k.om1, input_pair(f, again, o));
          const df t = two_sum(tm.h, a.h);
          df out = {t.h, fadd(t.l, fadd(tm.l, fadd(fsub(A.l, B.l), a.l)))};
-         if (FORCE) {
+         if (FORCE == 1) {
             const df fr = two_sum(sym.h, -k.Kf[s].h);
             const df t2 = two_sum(out.h, fr.h);
             out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fsub(sym.l, k.Kf[s].l))))};
@@ -628,7 +672,7 @@ struct EmitToArray {
 
 // The fast path on bits[] in place: returns false, leaving bits[] untouched,
 // when the cell must take the exact path.
-template <int Q, bool FORCE>
+template <int Q, int FORCE>
 __host__ __device__ __forceinline__ bool collide_f64x_fast(uint64_t (&bits)[Q], const x64::Consts& k,
                                                           int compat)
 {
@@ -679,8 +723,9 @@ template <int Q>
 __device__ __forceinline__ void collide_f64x(uint64_t (&bits)[Q], const KParams& p)
 {
    const x64::Consts k = collide_consts<Q>(p);
-   const bool fast = p.forced ? collide_f64x_fast<Q, true>(bits, k, p.compat)
-                              : collide_f64x_fast<Q, false>(bits, k, p.compat);
+   const bool fast = p.forced == 2 ? collide_f64x_fast<Q, 2>(bits, k, p.compat)
+                     : p.forced    ? collide_f64x_fast<Q, 1>(bits, k, p.compat)
+                                   : collide_f64x_fast<Q, 0>(bits, k, p.compat);
    if (fast) return;
    collide_exact_bits<Q>(bits, p);
 }
@@ -696,8 +741,9 @@ __device__ __forceinline__ void collide_f64x_shared(const unsigned long long* in
 #pragma unroll
    for (int s = 0; s < Q; s++) bits[s] = in[s * 32];
    const x64::Consts k = collide_consts<Q>(p);
-   const bool fast = p.forced ? collide_f64x_fast<Q, true>(bits, k, p.compat)
-                              : collide_f64x_fast<Q, false>(bits, k, p.compat);
+   const bool fast = p.forced == 2 ? collide_f64x_fast<Q, 2>(bits, k, p.compat)
+                     : p.forced    ? collide_f64x_fast<Q, 1>(bits, k, p.compat)
+                                   : collide_f64x_fast<Q, 0>(bits, k, p.compat);
    if (fast) return;
    const uint32_t a = (uint32_t)__cvta_generic_to_shared(in);
 #pragma unroll
@@ -740,8 +786,9 @@ __device__ __forceinline__ void collide_f64x_shared_emit(const unsigned long lon
    for (int s = 0; s < Q; s++) bits[s] = in[s * 32];
    const x64::Consts k = collide_consts<Q>(p);
    const AgainFromShared again{(uint32_t)__cvta_generic_to_shared(in)};
-   const bool fast = p.forced ? collide_f64x_fast_emit<Q, true>(bits, k, p.compat, emit, again)
-                              : collide_f64x_fast_emit<Q, false>(bits, k, p.compat, emit, again);
+   const bool fast = p.forced == 2 ? collide_f64x_fast_emit<Q, 2>(bits, k, p.compat, emit, again)
+                     : p.forced    ? collide_f64x_fast_emit<Q, 1>(bits, k, p.compat, emit, again)
+                                   : collide_f64x_fast_emit<Q, 0>(bits, k, p.compat, emit, again);
    if (fast) return;
 #pragma unroll
    for (int s = 0; s < Q; s++) bits[s] = again.raw(s);

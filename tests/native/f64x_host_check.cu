@@ -9,8 +9,14 @@
 
 namespace {
 
+int force_mode_of(const double* F, double omega)
+{
+   const double f[3] = {F[0], F[1], F[2]};
+   return lbm::force_mode(f, omega);
+}
+
 template <int Q>
-int run(const double* in, double* out, int n, double omega, const double* F, int compat, int* fast)
+int run(const double* in, double* out, int n, double omega, const double* F, int compat, int force_mode, int* fast)
 {
    using namespace lbm;
    x64::Consts k;
@@ -36,13 +42,14 @@ int run(const double* in, double* out, int n, double omega, const double* F, int
    }
    k.om2w36 = x64::df_from_double((1.0 - 0.5 * omega) / 36.0);
    k.om2 = (float)(1.0 - 0.5 * omega);
-   const bool forced = F[0] != 0.0 || F[1] != 0.0 || F[2] != 0.0;
+   const int mode = force_mode < 0 ? force_mode_of(F, omega) : force_mode;
    int nfast = 0;
    for (int i = 0; i < n; i++) {
       uint64_t bits[Q];
       for (int s = 0; s < Q; s++) bits[s] = x64::double_bits(in[(size_t)i * Q + s]);
-      const bool ok = forced ? collide_f64x_fast<Q, true>(bits, k, compat)
-                             : collide_f64x_fast<Q, false>(bits, k, compat);
+      const bool ok = mode == 2 ? collide_f64x_fast<Q, 2>(bits, k, compat)
+                    : mode == 1 ? collide_f64x_fast<Q, 1>(bits, k, compat)
+                                : collide_f64x_fast<Q, 0>(bits, k, compat);
       fast[i] = ok ? 1 : 0;
       nfast += ok;
       for (int s = 0; s < Q; s++)
@@ -53,8 +60,11 @@ int run(const double* in, double* out, int n, double omega, const double* F, int
 
 }  // namespace
 
+// force_mode: the fast path's forcing form (0, 1, 2 as lbm::force_mode), or
+// -1 for the one the library picks for this force and omega.
 extern "C" int f64x_collide_host(int Q, const double* in, double* out, int n, double omega, const double* F,
-                                 int compat, int* fast)
+                                 int compat, int force_mode, int* fast)
 {
-   return Q == 19 ? run<19>(in, out, n, omega, F, compat, fast) : run<27>(in, out, n, omega, F, compat, fast);
+   return Q == 19 ? run<19>(in, out, n, omega, F, compat, force_mode, fast)
+                  : run<27>(in, out, n, omega, F, compat, force_mode, fast);
 }

@@ -25,7 +25,8 @@ def f64x(tmp_path_factory):
                     "-o", str(out)], check=True)
     lib = ctypes.CDLL(str(out))
     P = ctypes.c_void_p
-    lib.f64x_collide_host.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_double, P, ctypes.c_int, P]
+    lib.f64x_collide_host.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_double, P, ctypes.c_int,
+                                      ctypes.c_int, P]
     return lib
 
 
@@ -55,22 +56,25 @@ def random_cells(Q, n, U, neq, seed):
     return f
 
 
-def run(lib, Q, f, omega, F, compat=0):
+def run(lib, Q, f, omega, F, compat=0, force_mode=-1):
+    """force_mode: 1 = forcing added after the equilibrium, 2 = folded into it
+    (small forces), -1 = the library's choice for this force and omega."""
     f = np.ascontiguousarray(f)
     out = np.empty_like(f)
     fast = np.empty(f.shape[0], np.int32)
     Fa = np.asarray(F, dtype=np.float64)
     lib.f64x_collide_host(Q, f.ctypes.data, out.ctypes.data, f.shape[0], omega, Fa.ctypes.data, compat,
-                          fast.ctypes.data)
+                          force_mode, fast.ctypes.data)
     return out, fast.astype(bool)
 
 
 @pytest.mark.parametrize("Q", [19, 27])
 @pytest.mark.parametrize("omega", [1.0 / 0.55, 1.25, 1.0, 0.7])
-@pytest.mark.parametrize("F", [(0.0, 0.0, 0.0), (1e-5, -2e-6, 3e-6)])
-def test_fast_path_matches_exact_collision(f64x, Q, omega, F):
+@pytest.mark.parametrize("F,mode", [((0.0, 0.0, 0.0), -1), ((1e-5, -2e-6, 3e-6), 1), ((1e-5, -2e-6, 3e-6), 2),
+                                    ((1e-3, 5e-4, -2e-4), 2), ((3e-2, -1e-2, 1e-2), 1)])
+def test_fast_path_matches_exact_collision(f64x, Q, omega, F, mode):
     f = random_cells(Q, 4000, 0.08, 0.02, seed=Q)
-    out, fast = run(f64x, Q, f, omega, F)
+    out, fast = run(f64x, Q, f, omega, F, force_mode=mode)
     assert fast.mean() > 0.99
     ref = collide_exact(Q, f, omega, F)
     err = np.abs(out[fast] - ref[fast]) / np.abs(ref[fast])
@@ -78,13 +82,28 @@ def test_fast_path_matches_exact_collision(f64x, Q, omega, F):
     assert np.median(err) < 2e-14
 
 
-def test_compat_rest_weight(f64x):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_compat_rest_weight(f64x, mode):
     f = random_cells(19, 500, 0.05, 0.01, seed=3)
     F = (1e-5, 0.0, 0.0)
-    out, fast = run(f64x, 19, f, 1.3, F, compat=1)
+    out, fast = run(f64x, 19, f, 1.3, F, compat=1, force_mode=mode)
     ref = collide_exact(19, f, 1.3, F, compat=True)
     assert fast.all()
     assert (np.abs(out - ref) / np.abs(ref)).max() < 2e-13
+
+
+def test_force_mode_choice(f64x):
+    """The folded form is picked only for sum |F_d| <= 0.004 omega; both forms
+    give the same results to F64X precision there."""
+    f = random_cells(27, 2000, 0.08, 0.02, seed=11)
+    for omega, F in ((1.0, (2e-3, 1e-3, 5e-4)), (0.5, (1e-3, 1e-3, 1e-5))):
+        auto, fa = run(f64x, 27, f, omega, F)
+        one, f1 = run(f64x, 27, f, omega, F, force_mode=1)
+        two, f2 = run(f64x, 27, f, omega, F, force_mode=2)
+        small = sum(abs(x) for x in F) <= 0.004 * omega
+        assert np.array_equal(auto[fa], (two if small else one)[fa])
+        assert (fa == f1).all() and (fa == f2).all()
+        assert (np.abs(one[fa] - two[fa]) / np.abs(one[fa])).max() < 2e-13
 
 
 @pytest.mark.parametrize("case", ["zero", "negative", "above_one", "fast_flow", "nan"])
