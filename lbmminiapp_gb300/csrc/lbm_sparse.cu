@@ -32,6 +32,7 @@
 
 #include "../../include/lbm_gb300.h"
 #include "lbm_f64x.cuh"
+#include "lbm_step_async.cuh"
 
 using namespace lbm;
 
@@ -112,10 +113,155 @@ __global__ void __launch_bounds__(kSparseThreads, sparse_min_blocks<Q>()) sparse
    }
 }
 
+// Pipelined form for F64X: persistent warps on tiles of 32 consecutive fluid
+// indices, the next tile's populations prefetched with 8-byte cp.async into a
+// two-stage shared buffer per warp while the current tile collides (the
+// dense grid's scheme, lbm_step_async.cuh).  The gather kinds (AA odd, AB
+// pull) need the next tile's adjacency to issue those copies, so each lane
+// loads it one tile further ahead into registers; the scatter kinds (AA odd,
+// AB push) load the current tile's write locations when its collision starts,
+// and each output is stored as the collision makes it.  AA stays race-free
+// under the prefetch: a fluid point's read and write locations are the same
+// set, disjoint from every other point's.
+constexpr int kSparseAsyncWarps = 4;
+constexpr int kSparseAsyncBlocks = 3;
+
+template <int KIND>
+constexpr bool sparse_gathers() { return KIND == K_AA_ODD || KIND == K_AB_PULL; }
+template <int KIND>
+constexpr bool sparse_scatters() { return KIND == K_AA_ODD || KIND == K_AB_PUSH; }
+
+template <int Q, int KIND>
+struct SparseEmit {
+   double* dst;
+   uint32_t nf, i;
+   const uint32_t (&wl)[Q];   // write locations (scatter kinds)
+   __device__ __forceinline__ void operator()(int s, uint64_t v) const
+   {
+      const uint32_t w = sparse_scatters<KIND>() ? wl[s] : nf * (uint32_t)s + i;
+      reinterpret_cast<unsigned long long*>(dst)[w] = v;
+   }
+};
+
+template <int Q, int KIND>
+__global__ void __launch_bounds__(kSparseAsyncWarps * 32, kSparseAsyncBlocks) sparse_async_kernel(
+   const KParams p, const int32_t* __restrict__ adj, uint32_t nf, uint32_t start, uint32_t count, uint32_t ntiles,
+   const double* src, double* dst)
+{
+   extern __shared__ __align__(16) unsigned long long sparse_smem[];
+   const int lane = threadIdx.x & 31;
+   const int warp = threadIdx.x >> 5;
+   const uint32_t nw = gridDim.x * kSparseAsyncWarps;
+   uint32_t t = blockIdx.x * kSparseAsyncWarps + warp;
+   if (t >= ntiles) return;
+   unsigned long long* mine = sparse_smem + (size_t)warp * kAsyncStages * Q * 32;
+   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
+   constexpr uint32_t kStageBytes = Q * 32 * 8;
+   const unsigned long long* s64 = reinterpret_cast<const unsigned long long*>(src);
+   // fluid index of this lane in tile tt, and whether it is inside the range
+   auto point = [&](uint32_t tt, bool& act) {
+      const uint32_t k = tt * 32u + (uint32_t)lane;
+      act = k < count;
+      return start + k;
+   };
+   uint32_t ahead[Q];   // read locations of the tile to be issued next (gather kinds)
+   auto load_ahead = [&](uint32_t tt) {
+      bool act;
+      const uint32_t i = point(tt, act);
+#pragma unroll
+      for (int s = 0; s < Q; s++) ahead[s] = act ? (uint32_t)__ldg(adj + (size_t)nf * s + i) : 0u;
+   };
+   auto issue = [&](uint32_t tt, uint32_t sb) {
+      bool act;
+      const uint32_t i = point(tt, act);
+      if (!act) return;
+#pragma unroll
+      for (int s = 0; s < Q; s++) {
+         uint32_t r;
+         if (KIND == K_AA_EVEN) r = nf * (uint32_t)lat_opp(Q, s) + i;
+         else if (KIND == K_AB_PUSH) r = nf * (uint32_t)s + i;
+         else r = ahead[s];
+         cp_async8(sb + (uint32_t)(s * 32 + lane) * 8u, s64 + r);
+      }
+   };
+   if (sparse_gathers<KIND>()) load_ahead(t);
+   issue(t, sbase);
+   cp_async_commit();
+   if (sparse_gathers<KIND>() && t + nw < ntiles) load_ahead(t + nw);
+   int stage = 0;
+   for (;;) {
+      const uint32_t next = t + nw;
+      if (next < ntiles) {
+         issue(next, sbase + (stage ^ 1) * kStageBytes);
+         if (sparse_gathers<KIND>() && next + nw < ntiles) load_ahead(next + nw);
+      }
+      cp_async_commit();
+      cp_async_wait_prev();
+      bool act;
+      const uint32_t i = point(t, act);
+      if (act) {
+         uint32_t wl[Q];
+         if (sparse_scatters<KIND>()) {
+#pragma unroll
+            for (int s = 0; s < Q; s++) {
+               const int r = KIND == K_AA_ODD ? lat_opp(Q, s) : s;
+               wl[s] = (uint32_t)__ldg(adj + (size_t)nf * r + i);
+            }
+         }
+         const SparseEmit<Q, KIND> emit{dst, nf, i, wl};
+         collide_f64x_shared_emit<Q>(mine + stage * Q * 32 + lane, p, emit);
+      }
+      if (next >= ntiles) break;
+      t = next;
+      stage ^= 1;
+   }
+}
+
+template <int Q, int KIND>
+cudaError_t launch_sparse_async(const KParams& p, const int32_t* adj, int64_t nfluid, int64_t start, int64_t count,
+                                const double* src, double* dst, cudaStream_t stream)
+{
+   // persistent grid per device ordinal, set once (any thread computes the same value)
+   static std::atomic<int> grid_of_device[64];
+   int dev = 0;
+   cudaError_t e = cudaGetDevice(&dev);
+   if (e != cudaSuccess) return e;
+   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+   auto kern = sparse_async_kernel<Q, KIND>;
+   constexpr size_t smem = (size_t)kSparseAsyncWarps * kAsyncStages * Q * 32 * sizeof(unsigned long long);
+   int cached = grid_of_device[dev].load(std::memory_order_relaxed);
+   if (cached == 0) {
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+      int per_sm = 0, nsm = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kSparseAsyncWarps * 32, smem);
+      if (e != cudaSuccess) return e;
+      e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      if (per_sm < 1) return cudaErrorInvalidConfiguration;
+      cached = per_sm * nsm;
+      grid_of_device[dev].store(cached, std::memory_order_relaxed);
+   }
+   const uint32_t ntiles = (uint32_t)((count + 31) / 32);
+   const uint32_t need = (ntiles + kSparseAsyncWarps - 1) / kSparseAsyncWarps;
+   const unsigned grid = (unsigned)(need < (uint32_t)cached ? need : (uint32_t)cached);
+   kern<<<grid, kSparseAsyncWarps * 32, smem, stream>>>(p, adj, (uint32_t)nfluid, (uint32_t)start, (uint32_t)count,
+                                                         ntiles, src, dst);
+   return cudaGetLastError();
+}
+
 template <int Q, int AR>
 cudaError_t launch_sparse_q(int kind, const KParams& p, const int32_t* adj, int64_t nfluid, int64_t start,
                             int64_t count, const double* src, double* dst, cudaStream_t stream)
 {
+   if (AR == AR_F64X) {
+      switch (kind) {
+         case K_AA_EVEN: return launch_sparse_async<Q, K_AA_EVEN>(p, adj, nfluid, start, count, src, dst, stream);
+         case K_AA_ODD: return launch_sparse_async<Q, K_AA_ODD>(p, adj, nfluid, start, count, src, dst, stream);
+         case K_AB_PUSH: return launch_sparse_async<Q, K_AB_PUSH>(p, adj, nfluid, start, count, src, dst, stream);
+         default: return launch_sparse_async<Q, K_AB_PULL>(p, adj, nfluid, start, count, src, dst, stream);
+      }
+   }
    const unsigned grid = (unsigned)((count + kSparseThreads - 1) / kSparseThreads);
    switch (kind) {
       case K_AA_EVEN:
