@@ -70,14 +70,23 @@ def test_f64x_within_1e10_of_reference(gpu, name):
     assert rel_err(out, g["raw_final"]) <= 1e-10
 
 
-@pytest.mark.parametrize("name", ["sparse_q19_aa_cylinder", "sparse_q19_ab_pull_cylinder"])
-def test_range_calls_compose(gpu, name):
+@pytest.mark.parametrize("arithmetic", ["f64", "f64x"])
+@pytest.mark.parametrize("name", ["sparse_q19_aa_cylinder", "sparse_q19_ab_pull_cylinder",
+                                  "sparse_q27_aa_cylinder"])
+def test_range_calls_compose(gpu, name, arithmetic):
+    """Border/bulk-style range calls (ranges not a multiple of the 32-point
+    tiles of the pipelined F64X kernel) equal one full-range call."""
     g = load_golden(name)
-    assert np.array_equal(run_case(g, "f64", chunks=3), g["raw_final"])
+    if arithmetic == "f64" and name in sparse_cases():
+        want = g["raw_final"]
+    else:
+        want = run_case(g, arithmetic)
+    assert np.array_equal(run_case(g, arithmetic, chunks=3), want)
 
 
+@pytest.mark.parametrize("arithmetic", ["f64", "f64x"])
 @pytest.mark.parametrize("name", ["sparse_q19_aa_cylinder", "sparse_q19_ab_push_cylinder"])
-def test_any_fluid_order(gpu, name):
+def test_any_fluid_order(gpu, name, arithmetic):
     """The same geometry in a shuffled fluid order gives the shuffled result."""
     g = load_golden(name)
     adj = g["adjacency"].astype(np.int64)
@@ -87,29 +96,31 @@ def test_any_fluid_order(gpu, name):
     inv[perm] = np.arange(n)
     s_part, j_part = np.divmod(adj[:, perm], n)
     adj_p = (s_part * n + inv[j_part]).astype(np.int32)
-    out = run_case(g, "f64", adjacency=adj_p)
-    assert np.array_equal(out, g["raw_final"][:, perm])
+    out = run_case(g, arithmetic, adjacency=adj_p)
+    want = g["raw_final"] if arithmetic == "f64" else run_case(g, arithmetic)
+    assert np.array_equal(out, want[:, perm])
 
 
-@pytest.mark.parametrize("pattern", ["aa", "ab_push", "ab_pull"])
-def test_matches_dense_layout_on_larger_cylinder(gpu, pattern):
+@pytest.mark.parametrize("arithmetic", ["f64", "f64x"])
+@pytest.mark.parametrize("Q,pattern", [(19, "aa"), (19, "ab_push"), (19, "ab_pull"), (27, "aa"), (27, "ab_pull")])
+def test_matches_dense_layout_on_larger_cylinder(gpu, Q, pattern, arithmetic):
     """build_adjacency + the compact kernels against the dense-layout path
-    (link words) on a size-1 cylinder, exact FP64 arithmetic: the same
-    populations bit for bit."""
+    (link words) on a size-1 cylinder: the same populations bit for bit, in
+    either arithmetic (both layouts run the same collision)."""
     import lbmminiapp_gb300 as lbm
     dims, solid = cylinder(1.0)
     nx, ny, nz = dims
-    cells, adj = sparse.build_adjacency(solid, (1, 0, 0), pattern, 19)
+    cells, adj = sparse.build_adjacency(solid, (1, 0, 0), pattern, Q)
     omega, gx, steps = 1.0 / 0.6, 1e-5, 9
-    with lbm.Simulation(nx, ny, nz, lattice=19, pattern=pattern, omega=omega, force=(gx, 0, 0),
-                        periodic=(1, 0, 0), arithmetic="f64") as sim:
+    with lbm.Simulation(nx, ny, nz, lattice=Q, pattern=pattern, omega=omega, force=(gx, 0, 0),
+                        periodic=(1, 0, 0), arithmetic=arithmetic) as sim:
         sim.set_solid(solid)
         sim.init_equilibrium(None, None)
         sim.step(steps)
-        dense = sim.get_populations("raw").reshape(19, -1)[:, cells]
-    g = dict(Q=19, prop_pattern=1 if pattern == "aa" else 0, pull=int(pattern == "ab_pull"), omega=omega,
+        dense = sim.get_populations("raw").reshape(Q, -1)[:, cells]
+    g = dict(Q=Q, prop_pattern=1 if pattern == "aa" else 0, pull=int(pattern == "ab_pull"), omega=omega,
              gx=gx, steps=steps, adjacency=adj)
-    out = run_case(g, "f64")
+    out = run_case(g, arithmetic)
     assert np.array_equal(out, dense)
 
 
