@@ -43,7 +43,7 @@ typedef enum lbm_status {
    LBM_ERR_OUT_OF_MEMORY = 2, /* device allocation failed or over max_device_bytes */
    LBM_ERR_CUDA = 3,          /* CUDA runtime error; see lbm_last_error */
    LBM_ERR_DIVERGED = 4,      /* NaN/Inf found by a conservation reduction */
-   LBM_ERR_UNSUPPORTED = 5,   /* valid request this build does not provide */
+   LBM_ERR_UNSUPPORTED = 5,   /* valid request the library does not provide */
    LBM_ERR_STATE = 6          /* call not valid in the handle's current state */
 } lbm_status;
 
