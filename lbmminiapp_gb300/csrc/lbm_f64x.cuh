@@ -448,18 +448,6 @@ __host__ __device__ constexpr int pair_dir(int Q, int p)
 // Fast-path validity thresholds (high words of the doubles).
 constexpr uint32_t kHiQuarter = (uint32_t)(1023 - 2) << 20;   // 0.25
 
-// The fast-path collision on one cell.  bits[] holds the Q input patterns in
-// direction order; each output pattern is handed to emit(s, pattern).
-// Returns false when the cell must take the exact path (nothing is emitted
-// when an input check fails; after an output check fails every output has
-// been emitted, possibly wrong):
-//   * inputs: rest population in [0.25, 1), the others in [2^-32, 0.25), and
-//     rho < 2;
-//   * |3 v_d| < 0.3: |c.u| stays well below 1 - uu/2, so the pair sums
-//     (1 - uu/2 + cu^2/2) +- cu keep their larger operand first;
-//   * outputs inside [2^-75, 1).
-// Work is organised by opposite pairs (s, opp(s)): cu, the quadratic term and
-// the omega*w*rho products are shared, since cu(opp) = -cu(s).
 template <int Q, class Again>
 __host__ __device__ __forceinline__ x64::df input_pair(const x64::df (&f)[Q], const Again& again, int s)
 {
@@ -474,6 +462,21 @@ struct KeepInputs {
    __host__ __device__ __forceinline__ x64::df operator()(int) const { return {0.f, 0.f}; }
 };
 
+// The fast-path collision on one cell.  bits[] holds the Q input patterns in
+// direction order; each output pattern is handed to emit(s, pattern).
+// Returns false when the cell must take the exact path (nothing is emitted
+// when an input check fails; after an output check fails every output has
+// been emitted, possibly wrong):
+//   * inputs: rest population in [0.25, 1), the others in [2^-32, 0.25), and
+//     rho < 2;
+//   * |3 v_d| < 0.3: |c.u| stays well below 1 - uu/2, so the pair sums
+//     (1 - uu/2 + cu^2/2) +- cu keep their larger operand first;
+//   * outputs inside [2^-75, 1).
+// Work is organised by opposite pairs (s, opp(s)): cu, the quadratic term and
+// the omega*w*rho products are shared, since cu(opp) = -cu(s).
+// FORCE is the forcing form of force_mode() (0 none, 1 added after the
+// equilibrium, 2 folded into it); Again supplies the inputs' float pairs for
+// the (1 - omega) f term (KeepInputs, or a second read from shared memory).
 template <int Q, int FORCE, class Emit, class Again>
 __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (&bits)[Q], const x64::Consts& k,
                                                                int compat, Emit& emit, const Again& again)
