@@ -733,31 +733,6 @@ __device__ __forceinline__ void collide_f64x(uint64_t (&bits)[Q], const KParams&
    collide_exact_bits<Q>(bits, p);
 }
 
-// The same for inputs that stay in shared memory (direction s at in[32 s]),
-// with the outputs left in bits[]: the fallback reads the inputs again from
-// there, so the input patterns need not stay in registers through the fast
-// path.
-template <int Q>
-__device__ __forceinline__ void collide_f64x_shared(const unsigned long long* in, uint64_t (&bits)[Q],
-                                                    const KParams& p)
-{
-#pragma unroll
-   for (int s = 0; s < Q; s++) bits[s] = in[s * 32];
-   const x64::Consts k = collide_consts<Q>(p);
-   const bool fast = p.forced == 2 ? collide_f64x_fast<Q, 2>(bits, k, p.compat)
-                     : p.forced    ? collide_f64x_fast<Q, 1>(bits, k, p.compat)
-                                   : collide_f64x_fast<Q, 0>(bits, k, p.compat);
-   if (fast) return;
-   const uint32_t a = (uint32_t)__cvta_generic_to_shared(in);
-#pragma unroll
-   for (int s = 0; s < Q; s++) {
-      unsigned long long v;
-      asm volatile("ld.shared.u64 %0, [%1];\n" : "=l"(v) : "r"(a + 256u * (uint32_t)s));
-      bits[s] = v;
-   }
-   collide_exact_bits<Q>(bits, p);
-}
-
 // Input pattern s read again from shared memory (direction s at byte 256 s
 // from the lane's first), raw or split into a float pair.  The load is
 // volatile so that the compiler does not keep the first load's value live in
@@ -774,7 +749,8 @@ struct AgainFromShared {
    __device__ __forceinline__ x64::df operator()(int s) const { return x64::split(raw(s)); }
 };
 
-// The same again, with each output handed to emit(s, pattern) as it is made, so neither the
+// collide_f64x for inputs that stay in shared memory (direction s at in[32 s]),
+// with each output handed to emit(s, pattern) as it is made, so neither the
 // input nor the output patterns stay in registers through the fast path: the
 // moment sums read the inputs once, the update reads them again.  If
 // the fast path fails after emitting, the exact results are emitted again

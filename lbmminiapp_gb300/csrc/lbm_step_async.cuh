@@ -33,13 +33,6 @@ constexpr int async_warps() { return Q == 19 ? 8 : 4; }
 template <int Q, int KIND>
 constexpr int async_min_blocks() { return async_warps<Q, KIND>() == 8 ? 2 : 3; }
 constexpr int kAsyncStages = 2;
-// Whether a step stores each output as the collision makes it (and re-reads
-// its inputs from shared memory for the update), which frees the registers
-// of Q input and Q output patterns; measured faster for every kind but the
-// D3Q27 AB steps, which keep their outputs in registers and store them after
-// the collision.
-template <int Q, int KIND>
-constexpr bool async_stream_out() { return !(Q == 27 && (KIND == K_AB_PUSH || KIND == K_AB_PULL)); }
 
 template <int Q, int KIND>
 constexpr size_t async_smem_bytes()
@@ -183,15 +176,11 @@ __global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<
       cp_async_commit();
       cp_async_wait_prev();
       if (!(LINKS || RAGGED) || cur.active) {
+         // each output is stored as the collision makes it, and the update
+         // re-reads its inputs from shared memory: neither the Q input nor the
+         // Q output patterns stay in registers
          StoreEmit<Q, KIND, LINKS> emit{pp, cur.ci, cur.lk};
-         if constexpr (async_stream_out<Q, KIND>()) {
-            collide_f64x_shared_emit<Q>(mine + stage * Q * 32 + lane, p, emit);
-         } else {
-            uint64_t bits[Q];
-            collide_f64x_shared<Q>(mine + stage * Q * 32 + lane, bits, p);
-#pragma unroll
-            for (int s = 0; s < Q; s++) emit(s, bits[s]);
-         }
+         collide_f64x_shared_emit<Q>(mine + stage * Q * 32 + lane, p, emit);
       }
       if (next >= ag.ntiles) break;
       t = next;
