@@ -323,11 +323,17 @@ struct JoinRange {
 };
 
 // Double pattern of h + l (positive):
-//   S  = h + l rounded toward zero, E = the remainder h + l - S (exact, >= 0);
-//   N  = E in units of one double ulp of S, an exact float below
-//        2^29 - 2^5 (E < ulp_float(S)), rounded to the nearest integer;
-//   the pattern of S as a double plus N: the double nearest to h + l.  S's
-//   double pattern has 29 zero low bits, so N goes in with an OR.
+//   S  = h + l rounded toward zero; the remainder h + l - S lies in
+//        [0, ulp_float(S)); E = l - (S - h) is that remainder rounded to a
+//        float (S - h is exact: S and h are within a factor of two).  The
+//        remainder of a rounded-toward-zero sum need not be a float: for a
+//        tiny negative l, S is h's predecessor and the remainder
+//        ulp_float(S) - |l| can round up to ulp_float(S) itself;
+//   N  = E in units of one double ulp of S, rounded to the nearest integer,
+//        at most 2^29 (one float ulp of S);
+//   the pattern of S as a double plus N (an integer add, which carries into
+//        the float part and the exponent when N reaches 2^29): within about
+//        33 double ulps of h + l.
 // S's pattern goes into `range`; the result is valid when range.ok().
 __host__ __device__ __forceinline__ uint64_t join(df v, JoinRange& range)
 {
@@ -337,7 +343,7 @@ __host__ __device__ __forceinline__ uint64_t join(df v, JoinRange& range)
    range.add(sb);
    const float scale = bitsf(0x99000000u - (sb & 0x7F800000u));  // 2^(52 - e(S))
    const uint32_t n = f2u_rn(fmul(E, scale));
-   return (((uint64_t)sb << 29) + ((uint64_t)0x38000000u << 32)) | n;
+   return (((uint64_t)sb << 29) + ((uint64_t)0x38000000u << 32)) + n;
 }
 
 __host__ __device__ __forceinline__ double as_double(uint64_t b)

@@ -146,3 +146,38 @@ def test_slow_flow_momentum_precision(f64x, Q, omega):
     c, _, _ = core.stencil(Q)
     mom = (out - ref) @ c.astype(float)
     assert np.sqrt((mom ** 2).mean()) < 8e-16
+
+
+def test_result_just_below_a_float_boundary(f64x):
+    """A result whose float-pair low part is a tiny negative (here direction
+    16: h = 0.0276889801, l = -5.6e-17) rounds toward zero to h's float
+    predecessor, and the remainder rounds up to one whole float ulp; that ulp
+    must carry into the double pattern.  (Found by a 4-million-cell sweep of
+    tau = 0.55 Taylor-Green-like cells, where it cost 6.7e-8 relative.)"""
+    cell = [float.fromhex(h) for h in (
+        "0x1.ae2c8324d2d6dp-5", "0x1.df4fd961ff843p-5", "0x1.e568aa7948808p-5", "0x1.a8adb322a2eaap-5",
+        "0x1.e51683e1d462dp-5", "0x1.a90b4b095a7e1p-5", "0x1.cbe4555e817e2p-6", "0x1.92844aa53813fp-6",
+        "0x1.cb7f469f0f6bdp-6", "0x1.92d239a1abce6p-6", "0x1.0025120996eccp-5", "0x1.c035ca2a223b1p-6",
+        "0x1.ffd4481221c61p-6", "0x1.c0b3caaa5da2ep-6", "0x1.0336a038a95a6p-5", "0x1.c677903f61c87p-6",
+        "0x1.c5a3e4f854109p-6", "0x1.8dc3c88c39b46p-6", "0x1.547e39b6a6ecdp-2")]
+    f = np.array([cell])
+    out, fast = run(f64x, 19, f, 1.0 / 0.55, (0.0, 0.0, 0.0))
+    ref = collide_exact(19, f, 1.0 / 0.55, (0.0, 0.0, 0.0))
+    assert fast.all()
+    assert (np.abs(out - ref) / np.abs(ref)).max() < 2e-13
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+def test_wide_sweep_of_flow_cells(f64x, Q):
+    """Two million cell updates of moderate flows near equilibrium at
+    tau = 0.55: every fast-path population within 2e-13 of the exact
+    collision."""
+    rng = np.random.default_rng(100 + Q)
+    n = 2_000_000 // Q
+    u = rng.uniform(-0.05, 0.05, (3, n)) + rng.uniform(-1e-3, 1e-3, (3, n))
+    f = core.equilibrium(Q, 1.0 + rng.uniform(-1e-3, 1e-3, n), u).T.copy()
+    f *= 1.0 + 1e-4 * rng.standard_normal(f.shape)
+    out, fast = run(f64x, Q, f, 1.0 / 0.55, (0.0, 0.0, 0.0))
+    ref = collide_exact(Q, f, 1.0 / 0.55, (0.0, 0.0, 0.0))
+    assert fast.all()
+    assert (np.abs(out - ref) / np.abs(ref)).max() < 2e-13
