@@ -15,7 +15,11 @@ is one lattice time step over the whole box (one kernel launch); the state is
 * roofline   HBM bound: algorithmic bytes 2*Q*8 = 304 B per fluid-cell update
              over the measured copy bandwidth (MEASURED_PEAKS.json);
 * cpu_baseline  the oracle port (C restatement of the reference's CPU kernels,
-             OpenMP on all host cores) on a bounded sample of the workload.
+             OpenMP on all host cores) on a bounded sample of the workload;
+* parity     the end-to-end run's result (F64X arithmetic, 1000 steps) against
+             the exact FP64 arithmetic on the same workload (the reference's
+             operation order, bit-identical to its CPU build): max relative
+             error of the populations, rho and u (bound 1e-10; one GPU only).
 
 ``--impl reference`` times that CPU implementation alone (each step one lattice
 step of a 256^3 sample of the same workload) and prints the same line shape.
@@ -40,6 +44,13 @@ sys.path.insert(0, str(ROOT))
 METRIC = "MLUPS (D3Q19 AA FP64, 512^3 Taylor-Green box)"
 UNIT = "MLUPS"
 TAU = 0.55
+# The port's speed against the reference's own CPU kernels, both on one thread
+# of the x86-64 build host (Xeon @ 2.70 GHz, 128^3 sample of this workload, 10
+# steps, two runs; the reference sources are not on the benchmark machine):
+# port 7.05 / 6.76 MLUPS, reference KernelAA_SOA_Unroll 6.33 / 6.93, Base 5.21 / 5.14.
+PORT_VS_REFERENCE = ("per thread the port runs 0.98-1.11x the reference's own AA Unroll kernel "
+                     "(KernelAA_SOA_Unroll.cpp, 6.3-6.9 MLUPS) and 1.3-1.4x its Base kernel on an x86-64 "
+                     "Xeon @ 2.70 GHz (128^3 sample of this workload)")
 
 
 def parse():
@@ -54,6 +65,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=1000,
                     help="lattice steps of the end-to-end round trip (the workload's 1000 steps)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the F64X-vs-exact-FP64 comparison of the end-to-end run (about 2 min at 512^3)")
     ap.add_argument("--ref-n", type=int, default=256, help="box edge of the reference arm's sample")
     ap.add_argument("--storage", default="f64", choices=["f64", "f32", "bf16", "f16"],
                     help="population storage of the timed run (headline: f64)")
@@ -321,6 +334,53 @@ def cylinder_benchmark(device, size=8.0, steps=20):
     return out
 
 
+def state_copy(sim):
+    """The handle's population buffer, copied into a new device tensor."""
+    import ctypes
+    import torch
+    t = torch.empty(int(sim.info.buffer_bytes), dtype=torch.uint8, device="cuda")
+    sim.synchronize()
+    torch.cuda.synchronize()
+    st = sim.lib.lbm_copy_state(sim.h, ctypes.c_void_p(t.data_ptr()), 0)
+    if st:
+        raise RuntimeError(f"lbm_copy_state failed ({st})")
+    sim.synchronize()
+    return t
+
+
+def parity_vs_exact(n, u0, steps, state_x, rho_x, u_x, device):
+    """The end-to-end run's F64X result against the exact FP64 arithmetic (the
+    reference's operation order, bit-identical to its CPU build) on the same
+    workload: max |a - b| / max |b| of the raw populations, rho and u."""
+    import torch
+    import lbmminiapp_gb300 as lbm
+    t0 = time.perf_counter()
+    with lbm.Simulation(n, n, n, lattice=19, pattern="aa", omega=1.0 / TAU, force=(0, 0, 0), storage="f64",
+                        arithmetic="f64", device=device) as sim:
+        sim.init_equilibrium(None, u0)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        sim.step(steps)
+        sim.synchronize()
+        exact_s = time.perf_counter() - t1
+        rho_e, u_e = sim.macros()
+        state_e = state_copy(sim)
+        plane = int(sim.info.plane_stride)
+    ncell = n ** 3
+    a = state_x.view(torch.float64).view(19, plane)[:, :ncell]
+    b = state_e.view(torch.float64).view(19, plane)[:, :ncell]
+    dmax = max(float((a[q] - b[q]).abs().max()) for q in range(19))
+    bmax = max(float(b[q].abs().max()) for q in range(19))
+    del a, b, state_e
+    return {"workload": f"D3Q19 AA {n}^3, tau {TAU}, Taylor-Green U 0.05 + 1e-3 noise, {steps} steps",
+            "compared": "F64X (the timed arithmetic) vs exact FP64 (reference operation order) on the GPU",
+            "pop_rel_max": dmax / bmax,
+            "rho_rel_max": float(np.abs(rho_x - rho_e).max() / np.abs(rho_e).max()),
+            "u_rel_max": float(np.abs(u_x - u_e).max() / np.abs(u_e).max()),
+            "tolerance": 1e-10, "exact_f64_mlups": round(ncell * steps / exact_s / 1e6, 1),
+            "seconds": round(time.perf_counter() - t0, 1)}
+
+
 def max_over_ranks(dist, value: float, device) -> float:
     """The largest `value` over all ranks (every rank gets it); `value` itself
     without a process group."""
@@ -359,7 +419,8 @@ def run_reference_arm(args, dist, rank, world):
                    "propagation": "AA", "grid": [n, n, n], "storage": "f64"},
         "cpu_baseline": {"value": round(mlups, 3), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n}^3 box, {args.steps} timed lattice steps; oracle/lbm_oracle.c "
-                                   "(C restatement of the reference's AA kernels, int32 adjacency, OpenMP)"},
+                                   "(C restatement of the reference's AA kernels, int32 adjacency, OpenMP); "
+                                   f"{PORT_VS_REFERENCE}"},
         "e2e": {"value": round(mlups, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -460,7 +521,16 @@ def main():
                "step": f"init_equilibrium(u from pinned host) + {steps_e2e} lattice steps + get_macros "
                        "(rho, u to pinned host)",
                "gpu_launches_per_step": launches_e2e}
-        del u_host, rho_out, u_out
+        del u_host
+    parity = None
+    if e2e is not None and arith == "f64x" and Q == 19 and args.pattern == "aa" and world == 1 \
+            and not args.no_parity:
+        state_x = state_copy(sim)
+        sim.close()
+        parity = parity_vs_exact(n, u, args.e2e_steps, state_x, rho_out.numpy(), u_out.numpy(), local)
+        del state_x
+    if e2e is not None:
+        del rho_out, u_out
     sim.close()
     del u
 
@@ -499,7 +569,7 @@ def main():
         cpu = {"value": round(mlups_cpu, 3), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{sample_n}^3 box of the same workload, {csteps} lattice steps in {csec:.1f} s; "
                          "oracle/lbm_oracle.c (C restatement of the reference AA kernels, int32 adjacency, "
-                         "OpenMP)"}
+                         f"OpenMP); {PORT_VS_REFERENCE}"}
 
     if rank == 0:
         line = {
@@ -520,6 +590,7 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "parity": parity,
             "variants": variants,
             "reference_benchmark": cylinder,
             "configs": configs,

@@ -169,7 +169,7 @@ lbm_status lbm_timestep_even_force(lbm_handle* h, void* dstrb, int64_t start, in
 /* KernelAA::timestepOddForce (src/kernels/KernelAA.hh:29) */
 lbm_status lbm_timestep_odd_force(lbm_handle* h, void* dstrb, int64_t start, int64_t count);
 /* KernelAB::timestepForce(Pdf* src, Pdf* tgt, int startIdx, int countIdx)
- * (src/kernels/KernelAB.hh:87); push or pull per cfg.pull */
+ * (src/kernels/KernelAB.hh:28); push or pull per cfg.pull */
 lbm_status lbm_timestep_force(lbm_handle* h, const void* src, void* tgt, int64_t start,
                               int64_t count);
 /* Device pointer of the handle's current population buffer (the one
@@ -237,7 +237,7 @@ lbm_status lbm_sparse_timestep_even_force(lbm_sparse_handle* h, double* dstrb, i
 /* KernelAA::timestepOddForce (src/kernels/KernelAA.hh:29) */
 lbm_status lbm_sparse_timestep_odd_force(lbm_sparse_handle* h, double* dstrb, int64_t start, int64_t count);
 /* KernelAB::timestepForce(Pdf* src, Pdf* tgt, int startIdx, int countIdx)
- * (src/kernels/KernelAB.hh:87); push or pull per cfg.pull */
+ * (src/kernels/KernelAB.hh:28); push or pull per cfg.pull */
 lbm_status lbm_sparse_timestep_force(lbm_sparse_handle* h, const double* src, double* tgt, int64_t start,
                                      int64_t count);
 
@@ -258,8 +258,10 @@ lbm_status lbm_sparse_timestep_force(lbm_sparse_handle* h, const double* src, do
  * most 2^28 (268,435,456) cells are accepted; larger grids return
  * LBM_ERR_INVALID_ARGUMENT.  The first call on each device looks the array's
  * address up (cudaGetSymbolAddress) with that device current; make that first
- * call before any stream capture.  All calls share the array: calls that
- * overlap on the GPU race. */
+ * call before any stream capture.  The address is kept for the life of the
+ * process, so calls must run in the device's primary context (the CUDA
+ * runtime's own) and the device must not be reset (cudaDeviceReset) between
+ * calls.  All calls share the array: calls that overlap on the GPU race. */
 lbm_status lbm_reduce_conserved_noalloc(int lattice, int storage, int nx, int ny, int nz,
                                         int64_t plane_stride, const void* dstrb, const uint8_t* solid,
                                         const int periodic[3], int readout, double* out, void* stream);

@@ -2,7 +2,8 @@
 
 A :class:`Rollout` runs ``steps`` AB-push lattice steps from a fixed initial
 state and accumulates a loss over a window of steps
-``window = (t0, t1)`` (the state after t steps, t0 <= t <= t1):
+``window = (t0, t1)`` (the state after t steps, t0 <= t <= t1, with
+0 <= t0 <= t1 <= steps; t = 0 is the initial state):
 
 * ``"velocity"``: time_weight * sum_x W(x) . u(x, t), W of shape (3, ...);
 * ``"energy"``:   time_weight * sum_x W(x) rho |u|^2 / 2, W of shape (...);
@@ -75,6 +76,8 @@ class Rollout:
         self.adjoint = adjoint
         self.kind = LOSS_KINDS[loss]
         self.t0, self.t1 = int(window[0]), int(window[1])
+        if not 0 <= self.t0 <= self.t1 <= self.steps:
+            raise ValueError(f"loss window {window} must satisfy 0 <= t0 <= t1 <= steps = {self.steps}")
         self.tw = float(time_weight)
         info = sim.info
         self.Q = sim.Q
@@ -96,6 +99,7 @@ class Rollout:
         self.ckpt = [self.init_state] + [self._alloc() for _ in range(nseg - 1)]
         self.final_state = self._alloc()
         self._pools = {}
+        self._torch_done()
 
     # ------------------------------------------------------------ helpers
     def _alloc(self):
@@ -110,6 +114,13 @@ class Rollout:
 
     def _check(self, st):
         N.check(st, self.h)
+
+    def _torch_done(self):
+        """Wait for torch's work on this device (fills of buffers the handle's
+        kernels read or accumulate into): the handle may run on another
+        stream than torch's current one."""
+        if self.dev.type == "cuda":
+            torch.cuda.current_stream(self.dev).synchronize()
 
     def to_plane(self, a, ncomp):
         """(ncomp, ncell)-shaped data -> (ncomp, plane) float64 device tensor."""
@@ -126,6 +137,7 @@ class Rollout:
         """force_field (3, ...) and porosity (...) on the grid; None removes."""
         self.force_field = None if force_field is None else self.to_plane(force_field.reshape(3, -1), 3)
         self.porosity = None if porosity is None else self.to_plane(porosity.reshape(1, -1), 1)
+        self._torch_done()
         self._check(self.lib.lbm_set_fields_device(self.h, _vp(self.force_field), _vp(self.porosity)))
 
     def _in_window(self, t):
@@ -148,6 +160,11 @@ class Rollout:
         self._load(self.init_state)
         loss = 0.0
         out = ctypes.c_double(0.0)
+        if self._in_window(0):
+            # the initial state's own term (its direct force dependence is
+            # differentiated by the adjoint step at t = 0)
+            self._check(self.lib.lbm_loss(self.h, None, self.kind, _vp(self.weight), self.tw, ctypes.byref(out)))
+            loss += out.value
         for t in range(self.steps):
             if store and t % self.K == 0 and t > 0:
                 self._save(self.ckpt[t // self.K])
@@ -204,6 +221,7 @@ class Rollout:
         self._lam = torch.zeros_like(self._lam_next)
         self._gF = torch.zeros((3, P), dtype=torch.float64, device=self.dev) if grad_force else None
         self._gS = torch.zeros((P,), dtype=torch.float64, device=self.dev)
+        self._torch_done()
         T = self.steps
         # seed: the final state's loss term (its direct force dependence
         # included); its buffer then serves the finest level's recomputation

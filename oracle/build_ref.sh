@@ -6,7 +6,8 @@
 # Test infrastructure only (the oracle): the outputs are git-ignored and are
 # used by tests/ to pin oracle/lbm_oracle.c and the golden fixtures against
 # the reference itself.  Needs the reference sources; exits 0 without building
-# when they are absent (LBM_REFERENCE_DIR overrides the default location).
+# when they are absent.  The sources are looked up in $LBM_REFERENCE_DIR, else in
+# a checkout named "reference" beside this repository.
 #
 #   -DSOA                 : the population layout the hot path uses
 #   -D_LATTICESIZE_=19|27 : one library per lattice (src/Parameters.hh:6-8)
@@ -15,7 +16,7 @@
 #   -include ref_overrides.h : run-time _OMEGA_ / _GRAVITY_ (see that header)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-REF="${LBM_REFERENCE_DIR:-/root/reference}"
+REF="${LBM_REFERENCE_DIR:-$(cd "$HERE/../.." && pwd)/reference}"
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src/kernels" ]; then
   echo "build_ref: reference sources not found at $REF; skipping" >&2

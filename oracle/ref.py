@@ -15,7 +15,9 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REF_DIR = Path(os.environ.get("LBM_REFERENCE_DIR", "/root/reference"))
+# The reference sources: $LBM_REFERENCE_DIR, else a checkout named "reference"
+# beside this repository.
+REF_DIR = Path(os.environ.get("LBM_REFERENCE_DIR", str(HERE.parents[1] / "reference")))
 OUT = HERE / "_ref"
 
 AA_BASE, AA_UNROLL, AB_PUSH_BASE, AB_PUSH_UNROLL, AB_PULL_BASE, AB_PULL_UNROLL = range(6)

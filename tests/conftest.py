@@ -19,3 +19,22 @@ def gpu():
     import lbmminiapp_gb300 as lbm
     lbm.lib()
     return lbm
+
+
+_PARITY = []
+
+
+@pytest.fixture
+def parity_record():
+    """record(name, {quantity: max relative error}): printed in the summary."""
+    def record(name, errs):
+        _PARITY.append((name, dict(errs)))
+    return record
+
+
+def pytest_terminal_summary(terminalreporter):
+    if not _PARITY:
+        return
+    terminalreporter.section("parity maxima (max |a - b| / max |b|)")
+    for name, errs in _PARITY:
+        terminalreporter.write_line(f"{name}: " + ", ".join(f"{k} {v:.2e}" for k, v in errs.items()))
