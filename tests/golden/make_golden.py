@@ -6,7 +6,8 @@ final raw population buffers as .npz files.  The reference sources are needed
 only to regenerate; the fixtures themselves are committed so parity checks run
 where the reference is absent.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # small cases
+    python tests/golden/make_golden.py --pins   # full-size C1 / C2 pins (about 25 min)
 """
 from __future__ import annotations
 
@@ -134,9 +135,55 @@ def make_vtk(tmpdir):
     print(f"{VTK_CASE}: {len(keep)} lines")
 
 
+# Reference pins of the full-size parity configurations.  The states are too
+# large to commit (C1 40 MB, C2 906 MB per pattern), so each fixture keeps the
+# SHA-256 of the reference's final populations over the fluid cells (the raw
+# buffer in (q, z, y, x) order, little-endian float64) and a seeded sample of
+# 1024 fluid cells.  The C1 initial state is rebuilt from 1-D tables of the
+# Taylor-Green factors stored in the fixture (tests/_helpers.py:tg_box_init), so
+# it does not depend on the host's libm.
+#   c1_q19_aa_tg64      64^3 periodic, D3Q19 AA Base, tau 0.8, rho 1, TG U 0.05, 200 steps
+#   c2_q27_ab_*_channel 256x128x128 channel (solid rows y = 0, 127), periodic x and z,
+#                       D3Q27 AB Base push / pull, gx 1e-6, tau 0.6, rest start, 1000 steps
+PIN_CASES = {
+    "pin_c1_q19_aa_tg64": dict(Q=19, variant=ref.AA_BASE, pattern=core.AA, dims=(64, 64, 64), periodic=(1, 1, 1),
+                               walls=False, tau=0.8, gx=0.0, steps=200, U=0.05),
+    "pin_c2_q27_ab_push_channel": dict(Q=27, variant=ref.AB_PUSH_BASE, pattern=core.AB_PUSH, dims=(256, 128, 128),
+                                       periodic=(1, 0, 1), walls=True, tau=0.6, gx=1e-6, steps=1000, U=0.0),
+    "pin_c2_q27_ab_pull_channel": dict(Q=27, variant=ref.AB_PULL_BASE, pattern=core.AB_PULL, dims=(256, 128, 128),
+                                       periodic=(1, 0, 1), walls=True, tau=0.6, gx=1e-6, steps=1000, U=0.0),
+}
+
+
+def make_pin(name):
+    from tests._helpers import fluid_digest, pin_init, tg_tables
+    c = PIN_CASES[name]
+    nx, ny, nz = c["dims"]
+    tables = tg_tables(nx, ny, nz) if c["U"] else {}
+    fix = dict(Q=c["Q"], pattern=c["pattern"], variant=c["variant"], dims=np.array(c["dims"]),
+               periodic=np.array(c["periodic"]), walls=int(c["walls"]), omega=1.0 / c["tau"], gx=c["gx"],
+               steps=c["steps"], U=c["U"], **tables)
+    f0, solid = pin_init(fix)
+    raw, sec = ref.box_run(c["Q"], c["variant"], f0, c["steps"], 1.0 / c["tau"], c["gx"], c["periodic"], solid)
+    fluid = ~solid.astype(bool)
+    idx = np.flatnonzero(fluid.ravel())
+    pick = np.sort(np.random.default_rng(11).choice(idx, 1024, replace=False))
+    np.savez_compressed(HERE / f"{name}.npz", **fix, init_sha256=fluid_digest(f0, solid),
+                        final_sha256=fluid_digest(raw, solid), sample_cells=pick,
+                        sample_f=raw.reshape(c["Q"], -1)[:, pick], ref_seconds=sec)
+    print(f"{name}: reference {sec:.1f} s, digest {fluid_digest(raw, solid)}", flush=True)
+
+
 def main():
     if not ref.available():
         sys.exit("reference harness unavailable (oracle/build_ref.sh needs the reference sources)")
+    if "--pins" in sys.argv:
+        # one process per case (the reference kernels are serial)
+        import multiprocessing as mp
+        names = [a for a in sys.argv[1:] if a in PIN_CASES] or list(PIN_CASES)
+        with mp.get_context("spawn").Pool(len(names)) as pool:
+            pool.map(make_pin, names)
+        return
     for name, (Q, variant, pattern, compat, dims, per, walls, tau, gx, steps, U, noise) in CASES.items():
         f0, solid = case_inputs(Q, dims, walls, U, noise)
         raw, _ = ref.box_run(Q, variant, f0, steps, 1.0 / tau, gx, per, solid)
