@@ -241,7 +241,8 @@ def config_benchmarks(device, steps=20):
     D3Q19 AA FP64 64^3 periodic Taylor-Green (tau 0.8);
     D3Q27 AB push / pull FP64 256x128x128 channel, gx 1e-6 (tau 0.6);
     D3Q19 AA FP32 128x64x64 channel with the smoothed porosity field, gx 1e-5 (tau 0.7);
-    D3Q27 AA FP16 384^3 sphere packing (solid fraction 0.35), gx 1e-6 (tau 0.7)."""
+    D3Q27 AA FP16 384^3 sphere packing (solid fraction 0.35), gx 1e-6 (tau 0.7), in the compact
+    fluid-only storage and on the dense grid."""
     import torch
     import lbmminiapp_gb300 as lbm
     from lbmminiapp_gb300 import workloads
@@ -276,11 +277,13 @@ def config_benchmarks(device, steps=20):
         sim.init_equilibrium()
         out["q19 aa f32 128x64x64 channel + porosity"] = timed(sim, 100)
     solid, _, _ = workloads.sphere_packing(384, 0.35, 6.0, 12.0, seed=2024)
-    with lbm.Simulation(384, 384, 384, lattice=27, pattern="aa", omega=1 / 0.7, force=(1e-6, 0, 0), storage="f16",
-                        device=device) as sim:
-        sim.set_solid(solid)
-        sim.init_equilibrium()
-        out["q27 aa f16 384^3 spheres"] = timed(sim, steps)
+    for compact in (True, False):
+        with lbm.Simulation(384, 384, 384, lattice=27, pattern="aa", omega=1 / 0.7, force=(1e-6, 0, 0),
+                            storage="f16", device=device, compact=compact) as sim:
+            sim.set_solid(solid)
+            sim.init_equilibrium()
+            name = "compact fluid-only storage" if compact else "dense grid"
+            out[f"q27 aa f16 384^3 spheres, {name}"] = timed(sim, steps)
     return out
 
 

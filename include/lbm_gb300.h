@@ -80,7 +80,10 @@ typedef struct lbm_config {
    int storage;       /* LBM_STORE_* */
    int arithmetic;    /* LBM_ARITH_* */
    int device;        /* CUDA device ordinal */
-   int reserved;
+   int compact;       /* 1: keep populations for fluid cells only (compact
+                         fluid-only storage; AA with F32/BF16/F16 storage),
+                         for media with many solid cells.  Host-facing arrays
+                         stay dense; no per-cell fields.  0: dense grid */
    uint64_t max_device_bytes; /* 0 = no cap; else creation fails with OOM above it */
 } lbm_config;
 

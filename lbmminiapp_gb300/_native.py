@@ -15,6 +15,8 @@ PKG = Path(__file__).resolve().parent
 LIB_PATH = PKG / "liblbm_gb300.so"
 
 LBM_OK = 0
+(LBM_ERR_INVALID_ARGUMENT, LBM_ERR_OUT_OF_MEMORY, LBM_ERR_CUDA, LBM_ERR_DIVERGED, LBM_ERR_UNSUPPORTED,
+ LBM_ERR_STATE) = range(1, 7)
 STATUS_NAMES = {
     0: "LBM_OK", 1: "LBM_ERR_INVALID_ARGUMENT", 2: "LBM_ERR_OUT_OF_MEMORY", 3: "LBM_ERR_CUDA",
     4: "LBM_ERR_DIVERGED", 5: "LBM_ERR_UNSUPPORTED", 6: "LBM_ERR_STATE",
@@ -36,7 +38,7 @@ class Config(ctypes.Structure):
         ("unroll", ctypes.c_int), ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int),
         ("periodic", ctypes.c_int * 3), ("omega", ctypes.c_double), ("force", ctypes.c_double * 3),
         ("storage", ctypes.c_int), ("arithmetic", ctypes.c_int), ("device", ctypes.c_int),
-        ("reserved", ctypes.c_int), ("max_device_bytes", ctypes.c_uint64),
+        ("compact", ctypes.c_int), ("max_device_bytes", ctypes.c_uint64),
     ]
 
 

@@ -30,6 +30,7 @@ SOURCES = [
     "lbm_step_q27_low.cu",
     "lbm_noalloc.cu",
     "lbm_sparse.cu",
+    "lbm_compact.cu",
     "lbm_adjoint.cu",
 ]
 

@@ -14,6 +14,7 @@
 #include "../../include/lbm_gb300.h"
 #include "lbm_adjoint.cuh"
 #include "lbm_aux.cuh"
+#include "lbm_compact.cuh"
 #include "lbm_dispatch.cuh"
 #include "lbm_f64x.cuh"
 
@@ -43,6 +44,23 @@ struct lbm_handle {
    double* partials = nullptr;     // reduction scratch: plane partials or 4 doubles per loss block
    double* reduce_out = nullptr;   // 4 doubles
    cudaStream_t stream = nullptr;
+   // Compact fluid-only storage (cfg.compact): the steps run on cbuf; buf[0]
+   // is the dense copy that set-up, readouts and host transfers use, brought
+   // up to date (expand / compress) when the other copy was written last.
+   bool compact = false;
+   void* cbuf = nullptr;
+   uint64_t cbuf_bytes = 0;
+   uint32_t nf32 = 0, cplane = 0, nrow_tiles = 0;
+   uint32_t* dcell = nullptr;       // [nf] dense cell of each fluid cell
+   uint32_t* ctile_first = nullptr;
+   uint32_t* ctile_row = nullptr;
+   RowInfo* crows = nullptr;        // [ny nz]
+   uint16_t* cpre = nullptr;        // [ncell]
+   uint16_t* cxs = nullptr;         // [nf]
+   uint32_t* clk = nullptr;         // [nf]
+   size_t compact_meta_bytes[7] = {0, 0, 0, 0, 0, 0, 0};
+   bool dense_current = true;       // buf[0] holds the latest state
+   bool compact_current = false;    // cbuf holds the latest state
    std::string err;
 };
 
@@ -269,6 +287,124 @@ int logical_mode(const lbm_handle* h)
 
 lbm_status check_handle(const lbm_handle* h) { return h ? LBM_OK : LBM_ERR_INVALID_ARGUMENT; }
 
+// Compact storage: make the dense copy current before it is read.
+lbm_status dense_for_read(lbm_handle* h)
+{
+   if (!h->compact || h->dense_current) return LBM_OK;
+   cudaError_t e = launch_compact_expand(h->Q, h->storage, h->dcell, h->nf32, h->cplane, h->cbuf, h->buf[0],
+                                         h->plane, h->stream);
+   if (e != cudaSuccess) return cuda_fail(h, e, "compact expand");
+   h->dense_current = true;
+   return LBM_OK;
+}
+
+// Compact storage: the dense copy was written; the compact one is stale.
+void dense_written(lbm_handle* h)
+{
+   h->dense_current = true;
+   h->compact_current = false;
+}
+
+CompactGeom compact_geom(const lbm_handle* h)
+{
+   CompactGeom g;
+   g.tile_first = h->ctile_first;
+   g.tile_row = h->ctile_row;
+   g.rows = h->crows;
+   g.pre = h->cpre;
+   g.xs = h->cxs;
+   g.lk = h->clk;
+   g.nrow_tiles = h->nrow_tiles;
+   g.nf = h->nf32;
+   g.cplane = h->cplane;
+   g.nx = h->cfg.nx;
+   g.ny = h->cfg.ny;
+   g.nz = h->cfg.nz;
+   g.m_ny = h->cfg.ny == 1 ? 0 : (~0ull / (uint64_t)h->cfg.ny) + 1;
+   return g;
+}
+
+void free_compact(lbm_handle* h)
+{
+   void* ptrs[7] = {h->dcell, h->ctile_first, h->ctile_row, h->crows, h->cpre, h->cxs, h->clk};
+   for (int k = 0; k < 7; k++) {
+      dev_free(h, ptrs[k], h->compact_meta_bytes[k]);
+      h->compact_meta_bytes[k] = 0;
+   }
+   h->dcell = h->ctile_first = h->ctile_row = h->clk = nullptr;
+   h->crows = nullptr;
+   h->cpre = h->cxs = nullptr;
+   dev_free(h, h->cbuf, h->cbuf_bytes);
+   h->cbuf = nullptr;
+   h->cbuf_bytes = 0;
+}
+
+// The compact numbering of the fluid cells (dense order, solids left out),
+// its row table, the per-cell prefix counts, the row tiles of the odd step
+// and the compact buffer, from the host mask (null: every cell fluid); the
+// link words are gathered from the dense ones.
+lbm_status build_compact(lbm_handle* h, const uint8_t* solid)
+{
+   const int nx = h->cfg.nx;
+   const int64_t nrows = (int64_t)h->cfg.ny * h->cfg.nz;
+   std::vector<uint32_t> dcell, tfirst, trow;
+   std::vector<RowInfo> rows((size_t)nrows);
+   std::vector<uint16_t> pre((size_t)h->ncell), xs;
+   dcell.reserve((size_t)h->nfluid);
+   xs.reserve((size_t)h->nfluid);
+   for (int64_t r = 0; r < nrows; r++) {
+      const uint32_t start = (uint32_t)dcell.size();
+      uint32_t cnt = 0;
+      for (int x = 0; x < nx; x++) {
+         const int64_t c = r * nx + x;
+         pre[(size_t)c] = (uint16_t)cnt;
+         if (!solid || !solid[c]) {
+            dcell.push_back((uint32_t)c);
+            xs.push_back((uint16_t)x);
+            cnt++;
+         }
+      }
+      rows[(size_t)r] = {start, cnt};
+      for (uint32_t k = 0; k < cnt; k += 32) {
+         tfirst.push_back(start + k);
+         trow.push_back((uint32_t)r);
+      }
+   }
+   free_compact(h);
+   h->nf32 = (uint32_t)dcell.size();
+   h->cplane = (h->nf32 + 255u) / 256u * 256u;
+   h->nrow_tiles = (uint32_t)tfirst.size();
+   if ((uint64_t)h->Q * h->cplane >= (1ull << 32))
+      return fail(h, LBM_ERR_UNSUPPORTED, "compact storage needs Q * fluid cells below 2^32");
+   struct Part {
+      void** dst;
+      const void* src;
+      size_t bytes;
+   } parts[7] = {{(void**)&h->dcell, dcell.data(), 4 * dcell.size()},
+                 {(void**)&h->ctile_first, tfirst.data(), 4 * tfirst.size()},
+                 {(void**)&h->ctile_row, trow.data(), 4 * trow.size()},
+                 {(void**)&h->crows, rows.data(), sizeof(RowInfo) * rows.size()},
+                 {(void**)&h->cpre, pre.data(), 2 * pre.size()},
+                 {(void**)&h->cxs, xs.data(), 2 * xs.size()},
+                 {(void**)&h->clk, nullptr, 4 * dcell.size()}};
+   for (int k = 0; k < 7; k++) {
+      const size_t bytes = std::max<size_t>(parts[k].bytes, 16);
+      lbm_status st = dev_alloc(h, parts[k].dst, bytes);
+      if (st != LBM_OK) return st;
+      h->compact_meta_bytes[k] = bytes;
+      if (parts[k].src && parts[k].bytes)
+         LBM_CUDA(h, cudaMemcpyAsync(*parts[k].dst, parts[k].src, parts[k].bytes, cudaMemcpyHostToDevice, h->stream));
+   }
+   LBM_CUDA(h, launch_compact_links(h->dcell, h->links, h->clk, h->nf32, h->stream));
+   h->cbuf_bytes = std::max<uint64_t>((uint64_t)h->cplane * h->Q * h->elem, 16);
+   lbm_status st = dev_alloc(h, &h->cbuf, h->cbuf_bytes);
+   if (st != LBM_OK) return st;
+   // the host vectors go out of scope: wait for the copies
+   LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   h->compact_current = false;
+   return LBM_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -334,6 +470,14 @@ void lbm_destroy(lbm_handle* h)
    }
    cudaFree(h->partials);
    cudaFree(h->reduce_out);
+   cudaFree(h->cbuf);
+   cudaFree(h->dcell);
+   cudaFree(h->ctile_first);
+   cudaFree(h->ctile_row);
+   cudaFree(h->crows);
+   cudaFree(h->cpre);
+   cudaFree(h->cxs);
+   cudaFree(h->clk);
    if (prev >= 0) cudaSetDevice(prev);
    delete h;
 }
@@ -361,6 +505,12 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_handle** out)
       st = fail(h, LBM_ERR_INVALID_ARGUMENT, "omega must lie in (0, 2)");
    else if (c.arithmetic < LBM_ARITH_AUTO || c.arithmetic > LBM_ARITH_F32)
       st = fail(h, LBM_ERR_INVALID_ARGUMENT, "unknown arithmetic");
+   else if (c.compact != 0 && c.compact != 1)
+      st = fail(h, LBM_ERR_INVALID_ARGUMENT, "compact must be 0 or 1");
+   else if (c.compact && (c.prop_pattern != LBM_PATTERN_AA || c.storage == LBM_STORE_F64))
+      st = fail(h, LBM_ERR_UNSUPPORTED, "compact storage runs AA steps with F32, BF16 or F16 storage");
+   else if (c.compact && c.nx > 65535)
+      st = fail(h, LBM_ERR_UNSUPPORTED, "compact storage needs nx <= 65535");
    if (st == LBM_OK) {
       h->Q = c.lattice;
       h->storage = c.storage;
@@ -374,6 +524,7 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_handle** out)
             st = fail(h, LBM_ERR_UNSUPPORTED, "shifted FP32/BF16/FP16 storage computes in FP32");
       }
       h->elem = c.storage == LBM_STORE_F64 ? 8 : (c.storage == LBM_STORE_F32 ? 4 : 2);
+      h->compact = c.compact != 0;
       h->ncell = ncell;
       h->nfluid = ncell;
       // Planes start on 512-byte boundaries.
@@ -447,6 +598,9 @@ lbm_status lbm_set_solid(lbm_handle* h, const uint8_t* solid)
 {
    if (!h) return LBM_ERR_INVALID_ARGUMENT;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   // the state carries over in the dense copy
+   lbm_status st0 = dense_for_read(h);
+   if (st0 != LBM_OK) return st0;
    int64_t nsolid = 0;
    if (solid)
       for (int64_t c = 0; c < h->ncell; c++) nsolid += solid[c] ? 1 : 0;
@@ -455,6 +609,7 @@ lbm_status lbm_set_solid(lbm_handle* h, const uint8_t* solid)
    if (!need_links) {
       dev_free(h, h->links, sizeof(uint32_t) * (size_t)h->ncell);
       h->links = nullptr;
+      if (h->compact) return build_compact(h, solid);
       return LBM_OK;
    }
    if (!h->links) {
@@ -473,6 +628,7 @@ lbm_status lbm_set_solid(lbm_handle* h, const uint8_t* solid)
    LBM_CUDA(h, cudaGetLastError());
    LBM_CUDA(h, cudaStreamSynchronize(h->stream));
    dev_free(h, sd, (size_t)h->ncell);
+   if (h->compact) return build_compact(h, solid);
    return LBM_OK;
 }
 
@@ -538,12 +694,14 @@ static lbm_status set_field(lbm_handle* h, const double* host, int ncomp, double
 lbm_status lbm_set_force_field(lbm_handle* h, const double* field)
 {
    if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->compact && field) return fail(h, LBM_ERR_UNSUPPORTED, "compact storage has no per-cell fields");
    return set_field(h, field, 3, &h->force_field, &h->force_field_f);
 }
 
 lbm_status lbm_set_porosity(lbm_handle* h, const double* porosity)
 {
    if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->compact && porosity) return fail(h, LBM_ERR_UNSUPPORTED, "compact storage has no per-cell fields");
    if (porosity)
       for (int64_t c = 0; c < h->ncell; c++)
          if (!(porosity[c] >= 0.0 && porosity[c] <= 1.0))
@@ -619,6 +777,7 @@ lbm_status lbm_init_equilibrium(lbm_handle* h, const double* rho, const double* 
    if (e != cudaSuccess) return cuda_fail(h, e, "init_eq sync");
    h->t = 0;
    h->cur = 0;
+   dense_written(h);
    return LBM_OK;
 }
 
@@ -645,6 +804,7 @@ lbm_status lbm_set_populations(lbm_handle* h, const double* f, int layout)
       LBM_CUDA(h, cudaGetLastError());
    }
    LBM_CUDA(h, cudaStreamSynchronize(h->stream));
+   dense_written(h);
    return LBM_OK;
 }
 
@@ -652,6 +812,8 @@ lbm_status lbm_get_populations(lbm_handle* h, double* f, int layout)
 {
    if (!h || !f || (layout != LBM_LAYOUT_RAW && layout != LBM_LAYOUT_LOGICAL)) return LBM_ERR_INVALID_ARGUMENT;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   lbm_status st = dense_for_read(h);
+   if (st != LBM_OK) return st;
    const int mode = layout == LBM_LAYOUT_RAW ? 0 : logical_mode(h);
    const void* buf = readout_buffer(h);
    for (int s = 0; s < h->Q; s++) {
@@ -664,10 +826,33 @@ lbm_status lbm_get_populations(lbm_handle* h, double* f, int layout)
    return LBM_OK;
 }
 
+// AA steps on the compact buffer.
+static lbm_status step_compact(lbm_handle* h, int nsteps)
+{
+   if (nsteps == 0) return LBM_OK;
+   if (!h->compact_current) {
+      LBM_CUDA(h, launch_compact_compress(h->Q, h->storage, h->dcell, h->nf32, h->cplane, h->buf[0], h->plane,
+                                          h->cbuf, h->stream));
+      h->compact_current = true;
+   }
+   h->dense_current = false;
+   Launch L;
+   const KParams p = make_params(h, 0, h->ncell, L);
+   const CompactGeom g = compact_geom(h);
+   for (int i = 0; i < nsteps; i++) {
+      const int kind = (h->t % 2 == 0) ? K_AA_EVEN : K_AA_ODD;
+      cudaError_t e = launch_compact_step(h->Q, h->storage, kind, p, g, h->cbuf, h->stream);
+      if (e != cudaSuccess) return cuda_fail(h, e, "compact step kernel launch");
+      h->t++;
+   }
+   return LBM_OK;
+}
+
 lbm_status lbm_step(lbm_handle* h, int nsteps)
 {
    if (!h || nsteps < 0) return LBM_ERR_INVALID_ARGUMENT;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   if (h->compact) return step_compact(h, nsteps);
    for (int i = 0; i < nsteps; i++) {
       lbm_status st;
       if (h->cfg.prop_pattern == LBM_PATTERN_AA) {
@@ -691,7 +876,8 @@ lbm_status lbm_get_macros(lbm_handle* h, double* rho, double* u)
    // The reference reads AA through the streamed populations and AB straight
    // from the stored buffer (src/propagation/PropagationAB.cpp:222-281).
    const int mode = h->cfg.prop_pattern == LBM_PATTERN_AA ? logical_mode(h) : 0;
-   lbm_status st = ensure_copy_stream(h);
+   lbm_status st = dense_for_read(h);
+   if (st == LBM_OK) st = ensure_copy_stream(h);
    if (st != LBM_OK) return st;
    const int64_t n = h->ncell;
    const int64_t chunk = chunk_cells(h, 4);
@@ -722,6 +908,8 @@ lbm_status lbm_reduce_conserved(lbm_handle* h, double out[4])
 {
    if (!h || !out) return LBM_ERR_INVALID_ARGUMENT;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   lbm_status st = dense_for_read(h);
+   if (st != LBM_OK) return st;
    dispatch_q_st<Conserved>(h->Q, h->storage, h, readout_buffer(h), logical_mode(h), h->partials,
                             h->reduce_out);
    LBM_CUDA(h, cudaGetLastError());
@@ -779,8 +967,14 @@ lbm_status lbm_copy_state(lbm_handle* h, void* dev, int to_handle)
    if (!h || !dev) return LBM_ERR_INVALID_ARGUMENT;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
    void* buf = const_cast<void*>(readout_buffer(h));
-   if (to_handle) LBM_CUDA(h, cudaMemcpyAsync(buf, dev, h->buffer_bytes, cudaMemcpyDeviceToDevice, h->stream));
-   else LBM_CUDA(h, cudaMemcpyAsync(dev, buf, h->buffer_bytes, cudaMemcpyDeviceToDevice, h->stream));
+   if (to_handle) {
+      LBM_CUDA(h, cudaMemcpyAsync(buf, dev, h->buffer_bytes, cudaMemcpyDeviceToDevice, h->stream));
+      dense_written(h);
+   } else {
+      lbm_status st = dense_for_read(h);
+      if (st != LBM_OK) return st;
+      LBM_CUDA(h, cudaMemcpyAsync(dev, buf, h->buffer_bytes, cudaMemcpyDeviceToDevice, h->stream));
+   }
    return LBM_OK;
 }
 
@@ -828,6 +1022,8 @@ static lbm_status set_field_device(lbm_handle* h, const double* dev, int ncomp, 
 lbm_status lbm_set_fields_device(lbm_handle* h, const double* force_field, const double* porosity)
 {
    if (!h) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->compact && (force_field || porosity))
+      return fail(h, LBM_ERR_UNSUPPORTED, "compact storage has no per-cell fields");
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
    lbm_status st = set_field_device(h, force_field, 3, &h->force_field, &h->force_field_f);
    if (st == LBM_OK) st = set_field_device(h, porosity, 1, &h->porosity, &h->porosity_f);
@@ -854,6 +1050,10 @@ lbm_status lbm_loss(lbm_handle* h, const void* state, int loss_kind, const doubl
    if (!h || !weight || !out_host || (loss_kind != LBM_LOSS_VELOCITY && loss_kind != LBM_LOSS_ENERGY))
       return LBM_ERR_INVALID_ARGUMENT;
    LBM_CUDA(h, cudaSetDevice(h->cfg.device));
+   if (!state) {
+      lbm_status st = dense_for_read(h);
+      if (st != LBM_OK) return st;
+   }
    AdjParams a = adj_params(h, state);
    a.loss_kind = loss_kind;
    a.loss_weight = weight;
@@ -911,6 +1111,8 @@ lbm_status lbm_adjoint_step_f32(lbm_handle* h, const void* state, const float* l
 lbm_status lbm_population_buffer(lbm_handle* h, void** dev_ptr)
 {
    if (!h || !dev_ptr) return LBM_ERR_INVALID_ARGUMENT;
+   if (h->compact)
+      return fail(h, LBM_ERR_UNSUPPORTED, "compact storage keeps its state in the compact buffer, not a dense one");
    *dev_ptr = const_cast<void*>(readout_buffer(h));
    return LBM_OK;
 }

@@ -45,13 +45,18 @@ def packing(n, solid_fraction=0.35, rmin=6.0, rmax=12.0, seed=0):
     return solid, len(radii)
 
 
-def forward(solid, tau, gx, steps, lattice=27, pattern="aa", storage="f16", arithmetic="auto", device=0):
+def forward(solid, tau, gx, steps, lattice=27, pattern="aa", storage="f16", arithmetic="auto", device=0,
+            compact=None):
     """Run ``steps`` steps from rest; returns a dict with the permeability, the
     mean velocity, the wall time of the steps and the fluid-cell update rate
-    (MFLUP/s)."""
+    (MFLUP/s).  compact: compact fluid-only storage (default: for AA with
+    shifted storage, the only case that has it)."""
     nz, ny, nx = solid.shape
+    if compact is None:
+        compact = pattern == "aa" and storage != "f64"
     with Simulation(nx, ny, nz, lattice=lattice, pattern=pattern, omega=1.0 / tau, force=(gx, 0.0, 0.0),
-                    periodic=(1, 1, 1), storage=storage, arithmetic=arithmetic, device=device) as sim:
+                    periodic=(1, 1, 1), storage=storage, arithmetic=arithmetic, device=device,
+                    compact=compact) as sim:
         sim.set_solid(solid)
         sim.init_equilibrium()
         sim.synchronize()

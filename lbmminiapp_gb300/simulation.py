@@ -19,7 +19,7 @@ PATTERNS = {"aa": (N.PATTERN_AA, 0), "ab_push": (N.PATTERN_AB, 0), "ab_pull": (N
 class Simulation:
     def __init__(self, nx, ny, nz, lattice=19, pattern="aa", omega=1.0, force=(0.0, 0.0, 0.0),
                  periodic=(1, 1, 1), storage="f64", arithmetic="auto", unroll=False, device=0,
-                 max_device_bytes=0):
+                 max_device_bytes=0, compact=False):
         if pattern not in PATTERNS:
             raise ValueError(f"pattern must be one of {sorted(PATTERNS)}")
         self.lib = N.lib()
@@ -37,6 +37,7 @@ class Simulation:
         cfg.arithmetic = N.ARITH_NAMES[arithmetic] if isinstance(arithmetic, str) else int(arithmetic)
         cfg.device = int(device)
         cfg.max_device_bytes = int(max_device_bytes)
+        cfg.compact = int(bool(compact))
         h = ctypes.c_void_p()
         st = self.lib.lbm_create(ctypes.byref(cfg), ctypes.byref(h))
         if st != N.LBM_OK:
