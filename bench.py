@@ -81,6 +81,9 @@ def parse():
                     help="print only the reference's cylinder benchmark (compact and dense layouts)")
     ap.add_argument("--configs", action="store_true",
                     help="print only the rates of the other workloads (small box, channel, porous channel, spheres)")
+    ap.add_argument("--spheres", type=int, default=0, metavar="N",
+                    help="print only the N^3 sphere-packing step rates (D3Q27 AA FP16, compact and dense), "
+                         "even and odd steps timed apart")
     ap.add_argument("--cylinder-size", type=float, default=8.0)
     ap.add_argument("--cylinder-steps", type=int, default=20)
     ap.add_argument("--porous-steps", type=int, default=2000)
@@ -287,6 +290,45 @@ def config_benchmarks(device, steps=20):
     return out
 
 
+def spheres_benchmark(device, n, steps=10):
+    """D3Q27 AA FP16 on the n^3 periodic sphere packing (radius 6-12, solid
+    fraction 0.35, seed 2024), gx 1e-6, tau 0.7: per step kind, the mean time
+    of `steps` launches (CUDA events around each) after 2 warm-up steps, as
+    fluid-cell GLUPS and GB/s of algorithmic traffic (108 B per fluid-cell
+    update), for the compact fluid-only storage and the dense grid."""
+    import torch
+    import lbmminiapp_gb300 as lbm
+    from lbmminiapp_gb300 import workloads
+    solid, _, _ = workloads.sphere_packing(n, 0.35, 6.0, 12.0, seed=2024)
+    out = {"workload": f"D3Q27 AA FP16 {n}^3 sphere packing, solid fraction {solid.mean():.3f}"}
+    for compact in (True, False):
+        with lbm.Simulation(n, n, n, lattice=27, pattern="aa", omega=1 / 0.7, force=(1e-6, 0, 0), storage="f16",
+                            device=device, compact=compact) as sim:
+            sim.set_solid(solid)
+            sim.init_equilibrium()
+            sim.step(2)
+            times = {0: [], 1: []}
+            for k in range(2 * steps):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                sim.step(1)
+                b.record()
+                b.synchronize()
+                times[k % 2].append(a.elapsed_time(b))
+            nf = sim.nfluid
+            res = {}
+            for kind, name in ((0, "even"), (1, "odd")):
+                ms = statistics.mean(times[kind])
+                res[name] = {"ms": round(ms, 4), "GLUPS": round(nf / (ms * 1e-3) / 1e9, 2),
+                             "GB/s": round(nf * 108 / (ms * 1e-3) / 1e9, 1)}
+            ms = statistics.mean(times[0] + times[1])
+            res["mean"] = {"ms": round(ms, 4), "GLUPS": round(nf / (ms * 1e-3) / 1e9, 2),
+                           "GB/s": round(nf * 108 / (ms * 1e-3) / 1e9, 1)}
+            out["compact" if compact else "dense"] = res
+            out["nfluid"] = nf
+    return out
+
+
 def cylinder_benchmark(device, size=8.0, steps=20):
     """The reference's own published benchmark workload: the size-8 cylinder
     (8,913,408 fluid points, src/geometries/Geometry.cpp:59-71,112-140),
@@ -456,6 +498,9 @@ def main():
         return 0
     if args.configs:
         print(json.dumps(config_benchmarks(local)), flush=True)
+        return 0
+    if args.spheres:
+        print(json.dumps(spheres_benchmark(local, args.spheres)), flush=True)
         return 0
     n = args.n
     ncell = n ** 3

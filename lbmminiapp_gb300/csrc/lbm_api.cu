@@ -321,6 +321,7 @@ CompactGeom compact_geom(const lbm_handle* h)
    g.ny = h->cfg.ny;
    g.nz = h->cfg.nz;
    g.m_ny = h->cfg.ny == 1 ? 0 : (~0ull / (uint64_t)h->cfg.ny) + 1;
+   for (int k = 0; k < 27; k++) g.soff[k] = (uint32_t)k * h->cplane;
    return g;
 }
 
@@ -399,6 +400,8 @@ lbm_status build_compact(lbm_handle* h, const uint8_t* solid)
    h->cbuf_bytes = std::max<uint64_t>((uint64_t)h->cplane * h->Q * h->elem, 16);
    lbm_status st = dev_alloc(h, &h->cbuf, h->cbuf_bytes);
    if (st != LBM_OK) return st;
+   // the plane padding past nf holds zeros (the even step's tail pair runs on it)
+   LBM_CUDA(h, cudaMemsetAsync(h->cbuf, 0, h->cbuf_bytes, h->stream));
    // the host vectors go out of scope: wait for the copies
    LBM_CUDA(h, cudaStreamSynchronize(h->stream));
    h->compact_current = false;

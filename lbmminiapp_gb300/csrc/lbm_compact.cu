@@ -31,10 +31,50 @@ namespace {
 
 constexpr int kCompactWarps = 8;
 
-template <int Q>
+// Two consecutive stored elements as one word: the even step's copy unit.
+template <typename T> struct PairWord;
+template <> struct PairWord<float> {
+   using W = uint2;
+   __device__ static void unpack(W w, float& a, float& b) { a = __uint_as_float(w.x); b = __uint_as_float(w.y); }
+   __device__ static W pack(float a, float b) { return make_uint2(__float_as_uint(a), __float_as_uint(b)); }
+};
+template <> struct PairWord<__half> {
+   using W = uint32_t;
+   __device__ static void unpack(W w, float& a, float& b)
+   {
+      const float2 f = __half22float2(*reinterpret_cast<const __half2*>(&w));
+      a = f.x;
+      b = f.y;
+   }
+   __device__ static W pack(float a, float b)
+   {
+      const __half2 h = __floats2half2_rn(a, b);
+      return *reinterpret_cast<const uint32_t*>(&h);
+   }
+};
+template <> struct PairWord<__nv_bfloat16> {
+   using W = uint32_t;
+   __device__ static void unpack(W w, float& a, float& b)
+   {
+      const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
+      a = f.x;
+      b = f.y;
+   }
+   __device__ static W pack(float a, float b)
+   {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+      return *reinterpret_cast<const uint32_t*>(&h);
+   }
+};
+
+// Shared memory per block: a two-stage buffer per warp of one word per lane
+// and direction (the even step's words hold two cells).
+template <int Q, int ST, int KIND>
 constexpr size_t compact_smem_bytes()
 {
-   return (size_t)kCompactWarps * kAsyncStages * Q * 32 * sizeof(uint32_t);
+   using T = typename Store<ST>::T;
+   return (size_t)kCompactWarps * kAsyncStages * Q * 32 *
+          (KIND == K_AA_EVEN ? sizeof(typename PairWord<T>::W) : sizeof(uint32_t));
 }
 
 // Address of the aligned 4-byte word holding element e (the element itself
@@ -64,27 +104,37 @@ __device__ __forceinline__ void collide_cell(const float (&G)[Q], float (&o)[Q],
 }
 
 // ------------------------------------------------------------------ even
+// Two cells per lane: tiles of 64 consecutive fluid indices, lane l takes
+// cells i0 = 64 t + 2 l and i0 + 1, whose slot-s elements form one aligned
+// word (i0 and the slot offsets are even).  A tail pair past nf runs on the
+// plane padding (cplane > nf, zero-filled), which no fluid cell reads.
 template <int Q, int ST, bool FORCE>
 __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_even_kernel(const KParams p, const CompactGeom g,
                                                                              typename Store<ST>::T* buf)
 {
    using T = typename Store<ST>::T;
+   using PW = PairWord<T>;
+   using W = typename PW::W;
    extern __shared__ __align__(16) uint32_t compact_smem[];
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
-   const uint32_t ntiles = (g.nf + 31) / 32;
+   const uint32_t ntiles = (g.nf + 63) / 64;
    const uint32_t nw = gridDim.x * kCompactWarps;
    uint32_t t = blockIdx.x * kCompactWarps + warp;
    if (t >= ntiles) return;
-   uint32_t* mine = compact_smem + (size_t)warp * kAsyncStages * Q * 32;
+   W* mine = reinterpret_cast<W*>(compact_smem) + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
-   constexpr uint32_t kStageBytes = Q * 32 * 4;
+   constexpr uint32_t kStageBytes = Q * 32 * sizeof(W);
    auto issue = [&](uint32_t tt, uint32_t sb) {
-      const uint32_t i = tt * 32 + lane;
-      if (i >= g.nf) return;
+      const uint32_t i0 = tt * 64 + 2 * (uint32_t)lane;
+      if (i0 >= g.nf) return;
 #pragma unroll
-      for (int s = 0; s < Q; s++)
-         cp_async4(sb + (uint32_t)(s * 32 + lane) * 4u, word_of(buf, (uint32_t)lat_opp(Q, s) * g.cplane + i));
+      for (int s = 0; s < Q; s++) {
+         const uint32_t dst = sb + (uint32_t)(s * 32 + lane) * (uint32_t)sizeof(W);
+         const T* src = buf + (g.soff[lat_opp(Q, s)] + i0);
+         if constexpr (sizeof(W) == 8) cp_async8(dst, src);
+         else cp_async4(dst, src);
+      }
    };
    issue(t, sbase);
    cp_async_commit();
@@ -94,18 +144,16 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_even_kernel(con
       if (next < ntiles) issue(next, sbase + (stage ^ 1) * kStageBytes);
       cp_async_commit();
       cp_async_wait_prev();
-      const uint32_t i = t * 32 + lane;
-      if (i < g.nf) {
-         // cplane is even, so every slot of cell i sits in the half of its
-         // word given by the parity of i
-         const bool high = (i & 1u) != 0u;
-         const uint32_t* sm = mine + stage * Q * 32;
-         float G[Q], o[Q];
+      const uint32_t i0 = t * 64 + 2 * (uint32_t)lane;
+      if (i0 < g.nf) {
+         const W* sm = mine + stage * Q * 32;
+         float G0[Q], G1[Q];
 #pragma unroll
-         for (int s = 0; s < Q; s++) G[s] = word_value<ST>(sm[s * 32 + lane], high);
-         collide_cell<Q, ST, FORCE>(G, o, p);
-#pragma unroll
-         for (int s = 0; s < Q; s++) store_raw(buf + ((uint32_t)s * g.cplane + i), o[s]);
+         for (int s = 0; s < Q; s++) PW::unpack(sm[s * 32 + lane], G0[s], G1[s]);
+         auto emit = [&](int s, float a, float b) {
+            *reinterpret_cast<W*>(buf + (g.soff[s] + i0)) = PW::pack(a, b);
+         };
+         collide2_f32_emit<Q, ST, FORCE>(G0, G1, p, emit);
       }
       if (next >= ntiles) break;
       t = next;
@@ -176,8 +224,8 @@ __device__ __forceinline__ uint32_t odd_issue(const T* buf, const CompactGeom& g
    for (int s = 0; s < Q; s++) {
       const int o = lat_opp(Q, s);
       uint32_t e;
-      if (s == lat_rest(Q) || ((L.lk >> o) & 1u)) e = (uint32_t)(s == lat_rest(Q) ? s : o) * g.cplane + L.i;
-      else e = (uint32_t)s * g.cplane + nbr_index<Q>(L, -lat_c(Q, s, 0), -lat_c(Q, s, 1), -lat_c(Q, s, 2));
+      if (s == lat_rest(Q) || ((L.lk >> o) & 1u)) e = g.soff[s == lat_rest(Q) ? s : o] + L.i;
+      else e = g.soff[s] + nbr_index<Q>(L, -lat_c(Q, s, 0), -lat_c(Q, s, 1), -lat_c(Q, s, 2));
       cp_async4(sb + (uint32_t)(s * 32 + lane) * 4u, word_of(buf, e));
       if constexpr (sizeof(T) == 2) halves |= (e & 1u) << s;
    }
@@ -232,8 +280,8 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(cons
 #pragma unroll
          for (int s = 0; s < Q; s++) {
             uint32_t e;
-            if (s == lat_rest(Q) || ((cur.lk >> s) & 1u)) e = (uint32_t)s * g.cplane + cur.i;
-            else e = (uint32_t)lat_opp(Q, s) * g.cplane + nbr_index<Q>(cur, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+            if (s == lat_rest(Q) || ((cur.lk >> s) & 1u)) e = g.soff[s] + cur.i;
+            else e = g.soff[lat_opp(Q, s)] + nbr_index<Q>(cur, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
             store_raw(buf + e, o[s]);
          }
       }
@@ -275,14 +323,14 @@ template <int Q, int ST, bool FORCE>
 cudaError_t launch_step_t(int kind, const KParams& p, const CompactGeom& g, void* buf, cudaStream_t stream)
 {
    using T = typename Store<ST>::T;
-   constexpr size_t smem = compact_smem_bytes<Q>();
+   const size_t smem = kind == K_AA_EVEN ? compact_smem_bytes<Q, ST, K_AA_EVEN>() : compact_smem_bytes<Q, ST, K_AA_ODD>();
    int grid = 0;
    uint32_t ntiles;
    cudaError_t e;
    if (kind == K_AA_EVEN) {
       static std::atomic<int> cache[64];
       e = persistent_grid(compact_even_kernel<Q, ST, FORCE>, smem, cache, grid);
-      ntiles = (g.nf + 31) / 32;
+      ntiles = (g.nf + 63) / 64;
    } else {
       static std::atomic<int> cache[64];
       e = persistent_grid(compact_odd_kernel<Q, ST, FORCE>, smem, cache, grid);

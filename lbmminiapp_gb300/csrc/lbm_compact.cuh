@@ -42,6 +42,7 @@ struct CompactGeom {
    uint32_t cplane;              // elements between direction planes (even, at least nf)
    int nx, ny, nz;
    uint64_t m_ny;                // ceil(2^64 / ny), 0 for ny = 1: row -> (y, z) by multiply-high
+   uint32_t soff[27];            // s * cplane: slot offsets in the parameter bank
 };
 
 // One AA step (kind K_AA_EVEN or K_AA_ODD) on a compact buffer.

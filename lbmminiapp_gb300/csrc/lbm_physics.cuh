@@ -181,48 +181,32 @@ __device__ __forceinline__ float cdot_f(const float (&v)[3])
    return r;
 }
 
-template <int Q, int ST, bool FORCE, int P = 0>
-__device__ __forceinline__ void collide_pairs_f32(const float (&G)[Q], float (&o)[Q], const float (&u3)[3],
-                                                  const float (&F3)[3], float fu, float uu, const float (&wSd)[4],
-                                                  const float (&wSr)[4], float om1, float omega, float Som2,
-                                                  int compat)
+// Representative s < opp(s) of the P-th opposite pair (the reference's
+// direction order: pairs (0,1), (2,3), ..., the rest direction last).
+template <int Q, int P>
+__host__ __device__ constexpr int pair_rep()
 {
-   if constexpr (P < (Q - 1) / 2) {
-      // representative s < opp(s) of the P-th pair
-      constexpr int s = [] {
-         int seen = 0;
-         for (int t = 0; t < Q; t++)
-            if (t < lat_opp(Q, t)) {
-               if (seen == P) return t;
-               seen++;
-            }
-         return -1;
-      }();
-      constexpr int ob = lat_opp(Q, s);
-      constexpr int cls = lat_norm2(Q, s);
-      const float cu = cdot_f<Q, s>(u3);
-      const float A = fmaf(wSr[cls], 0.5f * fmaf(cu, cu, -uu), wSd[cls]);
-      const float B = wSr[cls] * cu;
-      float fs = 0.0f, fo = 0.0f;
-      if (FORCE) {
-         constexpr float w = (float)lat_w(Q, s);
-         const float cf = cdot_f<Q, s>(F3);
-         const float sym = fmaf(cu, cf, -fu);
-         fs = Som2 * w * (cf + sym);
-         fo = Som2 * w * (sym - cf);
+   int seen = 0;
+   for (int t = 0; t < Q; t++)
+      if (t < lat_opp(Q, t)) {
+         if (seen == P) return t;
+         seen++;
       }
-      o[s] = fmaf(om1, G[s], fmaf(omega, A + B, fs));
-      o[ob] = fmaf(om1, G[ob], fmaf(omega, A - B, fo));
-      collide_pairs_f32<Q, ST, FORCE, P + 1>(G, o, u3, F3, fu, uu, wSd, wSr, om1, omega, Som2, compat);
-   }
+   return -1;
 }
 
+// Per-cell quantities of the shifted collision: 3u, 3F, fu = 3 F.u, uu = 3 u.u
+// and the weight-class factors w S drho, w S rho.
+struct ShiftedCell {
+   float u3[3], F3[3], fu, uu, wSd[4], wSr[4];
+};
+
 template <int Q, int ST, bool FORCE>
-__device__ __forceinline__ void collide_f32(const float (&G)[Q], float (&o)[Q], float F0, float F1, float F2,
-                                            float sp, const KParams& p)
+__device__ __forceinline__ ShiftedCell shifted_cell(const float (&G)[Q], float F0, float F1, float F2)
 {
    constexpr float S = ShiftScale<ST>::S;
    constexpr float iS = 1.0f / S;
+   ShiftedCell c;
    float Sd = 0.f, j0 = 0.f, j1 = 0.f, j2 = 0.f;
 #pragma unroll
    for (int s = 0; s < Q; s++) {
@@ -236,38 +220,120 @@ __device__ __forceinline__ void collide_f32(const float (&G)[Q], float (&o)[Q], 
    const float ir = __frcp_rn(rho);
    // 3u and 3F
    const float ir3 = 3.0f * ir;
-   float u3[3] = {fmaf(j0, iS, 0.5f * F0) * ir3, fmaf(j1, iS, 0.5f * F1) * ir3, fmaf(j2, iS, 0.5f * F2) * ir3};
-   const float uu = (u3[0] * u3[0] + u3[1] * u3[1] + u3[2] * u3[2]) * (1.0f / 3.0f);   // 3 u.u
-   float F3[3] = {3.0f * F0, 3.0f * F1, 3.0f * F2};
-   const float fu = FORCE ? (F3[0] * u3[0] + F3[1] * u3[1] + F3[2] * u3[2]) * (1.0f / 3.0f) : 0.0f;
+   c.u3[0] = fmaf(j0, iS, 0.5f * F0) * ir3;
+   c.u3[1] = fmaf(j1, iS, 0.5f * F1) * ir3;
+   c.u3[2] = fmaf(j2, iS, 0.5f * F2) * ir3;
+   c.uu = (c.u3[0] * c.u3[0] + c.u3[1] * c.u3[1] + c.u3[2] * c.u3[2]) * (1.0f / 3.0f);   // 3 u.u
+   c.F3[0] = 3.0f * F0;
+   c.F3[1] = 3.0f * F1;
+   c.F3[2] = 3.0f * F2;
+   c.fu = FORCE ? (c.F3[0] * c.u3[0] + c.F3[1] * c.u3[1] + c.F3[2] * c.u3[2]) * (1.0f / 3.0f) : 0.0f;
    const float Sr = S * rho;
-   float wSd[4], wSr[4];
 #pragma unroll
-   for (int c = 0; c < 4; c++) {
+   for (int k = 0; k < 4; k++) {
       float w;
-      if (Q == 19) w = c == 0 ? (float)(1.0 / 3.0) : (c == 1 ? (float)(1.0 / 18.0) : (float)(1.0 / 36.0));
-      else w = c == 0 ? (float)(8.0 / 27.0) : (c == 1 ? (float)(2.0 / 27.0) : (c == 2 ? (float)(1.0 / 54.0) : (float)(1.0 / 216.0)));
-      wSd[c] = w * Sd;
-      wSr[c] = w * Sr;
+      if (Q == 19) w = k == 0 ? (float)(1.0 / 3.0) : (k == 1 ? (float)(1.0 / 18.0) : (float)(1.0 / 36.0));
+      else w = k == 0 ? (float)(8.0 / 27.0) : (k == 1 ? (float)(2.0 / 27.0) : (k == 2 ? (float)(1.0 / 54.0) : (float)(1.0 / 216.0)));
+      c.wSd[k] = w * Sd;
+      c.wSr[k] = w * Sr;
    }
-   const float Som2 = S * p.om2f;
-   collide_pairs_f32<Q, ST, FORCE>(G, o, u3, F3, fu, uu, wSd, wSr, p.om1f, p.omegaf, Som2, p.compat);
-   // rest: A = w (S drho + S rho (-uu/2)), forcing -wf fu
+   return c;
+}
+
+// Outputs of the P-th pair (s, opp(s)) from the inputs Gs, Gob.
+template <int Q, int ST, bool FORCE, int P>
+__device__ __forceinline__ void shifted_pair(const ShiftedCell& c, float Gs, float Gob, float om1, float omega,
+                                             float Som2, float& os, float& oob)
+{
+   constexpr int s = pair_rep<Q, P>();
+   constexpr int cls = lat_norm2(Q, s);
+   const float cu = cdot_f<Q, s>(c.u3);
+   const float A = fmaf(c.wSr[cls], 0.5f * fmaf(cu, cu, -c.uu), c.wSd[cls]);
+   const float B = c.wSr[cls] * cu;
+   float fs = 0.0f, fo = 0.0f;
+   if (FORCE) {
+      constexpr float w = (float)lat_w(Q, s);
+      const float cf = cdot_f<Q, s>(c.F3);
+      const float sym = fmaf(cu, cf, -c.fu);
+      fs = Som2 * w * (cf + sym);
+      fo = Som2 * w * (sym - cf);
+   }
+   os = fmaf(om1, Gs, fmaf(omega, A + B, fs));
+   oob = fmaf(om1, Gob, fmaf(omega, A - B, fo));
+}
+
+// Output of the rest direction: A = w (S drho + S rho (-uu/2)), forcing -wf fu.
+template <int Q, int ST, bool FORCE>
+__device__ __forceinline__ float shifted_rest(const ShiftedCell& c, float GR, const KParams& p, float Som2)
+{
+   const float A = fmaf(c.wSr[0], -0.5f * c.uu, c.wSd[0]);
+   float fr = 0.0f;
+   if (FORCE) {
+      const float wf = (Q == 19 && p.compat) ? (float)(1.0 / 36.0) : (float)lat_w(Q, lat_rest(Q));
+      fr = -Som2 * wf * c.fu;
+   }
+   return fmaf(p.om1f, GR, fmaf(p.omegaf, A, fr));
+}
+
+template <int Q, int ST, bool FORCE, int P = 0>
+__device__ __forceinline__ void collide_pairs_f32(const float (&G)[Q], float (&o)[Q], const ShiftedCell& c, float om1,
+                                                  float omega, float Som2)
+{
+   if constexpr (P < (Q - 1) / 2) {
+      constexpr int s = pair_rep<Q, P>();
+      constexpr int ob = lat_opp(Q, s);
+      shifted_pair<Q, ST, FORCE, P>(c, G[s], G[ob], om1, omega, Som2, o[s], o[ob]);
+      collide_pairs_f32<Q, ST, FORCE, P + 1>(G, o, c, om1, omega, Som2);
+   }
+}
+
+template <int Q, int ST, bool FORCE>
+__device__ __forceinline__ void collide_f32(const float (&G)[Q], float (&o)[Q], float F0, float F1, float F2,
+                                            float sp, const KParams& p)
+{
+   const ShiftedCell c = shifted_cell<Q, ST, FORCE>(G, F0, F1, F2);
+   const float Som2 = ShiftScale<ST>::S * p.om2f;
+   collide_pairs_f32<Q, ST, FORCE>(G, o, c, p.om1f, p.omegaf, Som2);
    constexpr int R = lat_rest(Q);
-   {
-      const float A = fmaf(wSr[0], -0.5f * uu, wSd[0]);
-      float fr = 0.0f;
-      if (FORCE) {
-         const float wf = (Q == 19 && p.compat) ? (float)(1.0 / 36.0) : (float)lat_w(Q, R);
-         fr = -Som2 * wf * fu;
-      }
-      o[R] = fmaf(p.om1f, G[R], fmaf(p.omegaf, A, fr));
-   }
+   o[R] = shifted_rest<Q, ST, FORCE>(c, G[R], p, Som2);
    if (sp != 0.0f) {
       const float keep = 1.0f - sp;
 #pragma unroll
       for (int s = 0; s < Q; s++) o[s] = keep * o[s] + sp * G[lat_opp(Q, s)];
    }
+}
+
+// Two cells (inputs G0, G1) with a uniform force: each direction's pair of
+// outputs goes to emit(s, o0, o1) as soon as it is made, so no output array
+// stays in registers.  The arithmetic per cell is collide_f32's.
+template <int Q, int ST, bool FORCE, int P = 0, class Emit2>
+__device__ __forceinline__ void collide2_pairs_f32(const float (&G0)[Q], const float (&G1)[Q], const ShiftedCell& c0,
+                                                   const ShiftedCell& c1, float om1, float omega, float Som2,
+                                                   Emit2& emit)
+{
+   if constexpr (P < (Q - 1) / 2) {
+      constexpr int s = pair_rep<Q, P>();
+      constexpr int ob = lat_opp(Q, s);
+      float a0, b0, a1, b1;
+      shifted_pair<Q, ST, FORCE, P>(c0, G0[s], G0[ob], om1, omega, Som2, a0, b0);
+      shifted_pair<Q, ST, FORCE, P>(c1, G1[s], G1[ob], om1, omega, Som2, a1, b1);
+      emit(s, a0, a1);
+      emit(ob, b0, b1);
+      collide2_pairs_f32<Q, ST, FORCE, P + 1>(G0, G1, c0, c1, om1, omega, Som2, emit);
+   }
+}
+
+template <int Q, int ST, bool FORCE, class Emit2>
+__device__ __forceinline__ void collide2_f32_emit(const float (&G0)[Q], const float (&G1)[Q], const KParams& p,
+                                                  Emit2& emit)
+{
+   const float F0 = FORCE ? p.Ff[0] : 0.0f, F1 = FORCE ? p.Ff[1] : 0.0f, F2 = FORCE ? p.Ff[2] : 0.0f;
+   const ShiftedCell c0 = shifted_cell<Q, ST, FORCE>(G0, F0, F1, F2);
+   const ShiftedCell c1 = shifted_cell<Q, ST, FORCE>(G1, F0, F1, F2);
+   const float Som2 = ShiftScale<ST>::S * p.om2f;
+   collide2_pairs_f32<Q, ST, FORCE>(G0, G1, c0, c1, p.om1f, p.omegaf, Som2, emit);
+   constexpr int R = lat_rest(Q);
+   emit(R, shifted_rest<Q, ST, FORCE>(c0, G0[R], p, Som2), shifted_rest<Q, ST, FORCE>(c1, G1[R], p, Som2));
 }
 
 }  // namespace lbm
