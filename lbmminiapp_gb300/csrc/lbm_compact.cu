@@ -24,6 +24,7 @@
 #include <atomic>
 
 #include "lbm_compact.cuh"
+#include "lbm_launch.cuh"
 #include "lbm_step_async_low.cuh"
 
 namespace lbm {
@@ -122,6 +123,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_even_kernel(con
    const uint32_t nw = gridDim.x * kCompactWarps;
    uint32_t t = blockIdx.x * kCompactWarps + warp;
    if (t >= ntiles) return;
+   wait_prior_grid();
    W* mine = reinterpret_cast<W*>(compact_smem) + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * sizeof(W);
@@ -243,6 +245,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(cons
    const uint32_t nw = gridDim.x * kCompactWarps;
    uint32_t t = blockIdx.x * kCompactWarps + warp;
    if (t >= ntiles) return;
+   wait_prior_grid();
    uint32_t* mine = compact_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 4;
@@ -341,9 +344,11 @@ cudaError_t launch_step_t(int kind, const KParams& p, const CompactGeom& g, void
    const uint32_t need = (ntiles + kCompactWarps - 1) / kCompactWarps;
    const unsigned blocks = (unsigned)(need < (uint32_t)grid ? need : (uint32_t)grid);
    T* b = static_cast<T*>(buf);
-   if (kind == K_AA_EVEN) compact_even_kernel<Q, ST, FORCE><<<blocks, kCompactWarps * 32, smem, stream>>>(p, g, b);
-   else compact_odd_kernel<Q, ST, FORCE><<<blocks, kCompactWarps * 32, smem, stream>>>(p, g, b);
-   return cudaGetLastError();
+   if (kind == K_AA_EVEN)
+      return launch_overlapped(compact_even_kernel<Q, ST, FORCE>, dim3(blocks), dim3(kCompactWarps * 32), smem, stream,
+                               p, g, b);
+   return launch_overlapped(compact_odd_kernel<Q, ST, FORCE>, dim3(blocks), dim3(kCompactWarps * 32), smem, stream, p,
+                            g, b);
 }
 
 template <int Q, int ST>

@@ -31,9 +31,11 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
    T* d = static_cast<T*>(dst);
    if constexpr (ST != ST_F64) {
       if (L.pair && !links && !fields) {
-         if (L.idx32) step_pair_kernel<Q, ST, KIND, uint32_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
-         else step_pair_kernel<Q, ST, KIND, int64_t><<<L.pair_grid, L.pair_block, 0, L.stream>>>(p, s, d);
-         return cudaGetLastError();
+         if (L.idx32)
+            return launch_overlapped(step_pair_kernel<Q, ST, KIND, uint32_t>, L.pair_grid, L.pair_block, 0, L.stream,
+                                     p, s, d);
+         return launch_overlapped(step_pair_kernel<Q, ST, KIND, int64_t>, L.pair_grid, L.pair_block, 0, L.stream, p,
+                                  s, d);
       }
       if (L.async_low && links && !fields) {
          const bool ragged = p.nx % 32 != 0;
@@ -55,16 +57,24 @@ cudaError_t launch_kind(const Launch& L, const KParams& p, const void* src, void
    // Per-cell fields (porosity, force field): 64-bit stride arithmetic only.
    // The plain step kernels get a 32-bit stride variant for planes below 4 GiB.
    if (fields) {
-      if (links) step_kernel<Q, ST, ARF, KIND, true, true, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
-      else step_kernel<Q, ST, ARF, KIND, false, true, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
-   } else if (L.idx32) {
-      if (links) step_kernel<Q, ST, AR, KIND, true, false, uint32_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
-      else step_kernel<Q, ST, AR, KIND, false, false, uint32_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
-   } else {
-      if (links) step_kernel<Q, ST, AR, KIND, true, false, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
-      else step_kernel<Q, ST, AR, KIND, false, false, int64_t><<<L.grid, L.block, 0, L.stream>>>(p, s, d);
+      if (links)
+         return launch_overlapped(step_kernel<Q, ST, ARF, KIND, true, true, int64_t>, L.grid, L.block, 0, L.stream, p,
+                                  s, d);
+      return launch_overlapped(step_kernel<Q, ST, ARF, KIND, false, true, int64_t>, L.grid, L.block, 0, L.stream, p, s,
+                               d);
    }
-   return cudaGetLastError();
+   if (L.idx32) {
+      if (links)
+         return launch_overlapped(step_kernel<Q, ST, AR, KIND, true, false, uint32_t>, L.grid, L.block, 0, L.stream, p,
+                                  s, d);
+      return launch_overlapped(step_kernel<Q, ST, AR, KIND, false, false, uint32_t>, L.grid, L.block, 0, L.stream, p,
+                               s, d);
+   }
+   if (links)
+      return launch_overlapped(step_kernel<Q, ST, AR, KIND, true, false, int64_t>, L.grid, L.block, 0, L.stream, p, s,
+                               d);
+   return launch_overlapped(step_kernel<Q, ST, AR, KIND, false, false, int64_t>, L.grid, L.block, 0, L.stream, p, s,
+                            d);
 }
 
 template <int Q, int ST, int AR>

@@ -20,6 +20,7 @@
 #pragma once
 
 #include "lbm_f64x.cuh"
+#include "lbm_launch.cuh"
 #include "lbm_physics.cuh"
 
 namespace lbm {
@@ -140,6 +141,7 @@ template <int Q, int ST, int AR, int KIND, bool LINKS, bool FIELDS, typename IT>
 __global__ void __launch_bounds__(256) step_kernel(const KParams p, const typename Store<ST>::T* src,
                                                    typename Store<ST>::T* dst)
 {
+   wait_prior_grid();
    CellIndex ci;
    if (!cell_of_thread(p, ci)) return;
    uint32_t lk = 0;
@@ -242,6 +244,7 @@ __global__ void __launch_bounds__(256, pair_min_blocks<Q, ST>()) step_pair_kerne
 {
    using T = typename Store<ST>::T;
    using PV = PairVec<T>;
+   wait_prior_grid();
    const int x0 = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
    if (x0 >= p.nx) return;
    const int y = blockIdx.y, z = p.z0 + blockIdx.z;

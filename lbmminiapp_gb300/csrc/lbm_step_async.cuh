@@ -20,6 +20,7 @@
 
 #include <atomic>
 
+#include "lbm_launch.cuh"
 #include "lbm_step.cuh"
 
 namespace lbm {
@@ -156,6 +157,7 @@ __global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<
    const uint32_t nw = gridDim.x * kWarps;
    uint32_t t = blockIdx.x * kWarps + warp;
    if (t >= ag.ntiles) return;
+   wait_prior_grid();
    unsigned long long* mine = async_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 8;
@@ -235,8 +237,7 @@ cudaError_t launch_async(const KParams& p, const AsyncGeom& ag, const void* src,
       pp.src[s] = static_cast<const unsigned long long*>(src) + (int64_t)k * p.plane;
       pp.dst[s] = static_cast<unsigned long long*>(dst) + (int64_t)k * p.plane;
    }
-   kern<<<grid, kWarps * 32, smem, stream>>>(p, ag, pp);
-   return cudaGetLastError();
+   return launch_overlapped(kern, dim3(grid), dim3(kWarps * 32), smem, stream, p, ag, pp);
 }
 
 }  // namespace lbm

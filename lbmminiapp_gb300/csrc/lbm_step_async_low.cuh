@@ -92,6 +92,7 @@ __global__ void __launch_bounds__(kAsyncLowWarps * 32) step_async_low_kernel(
    const uint32_t nw = gridDim.x * kAsyncLowWarps;
    uint32_t t = blockIdx.x * kAsyncLowWarps + warp;
    if (t >= ag.ntiles) return;
+   wait_prior_grid();
    uint32_t* mine = async_low_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 4;
@@ -167,8 +168,7 @@ cudaError_t launch_async_low(const KParams& p, const AsyncGeom& ag, const void* 
    pp.src = static_cast<const T*>(src);
    pp.dst = static_cast<T*>(dst);
    pp.plane = (uint32_t)p.plane;
-   kern<<<grid, kAsyncLowWarps * 32, smem, stream>>>(p, ag, pp);
-   return cudaGetLastError();
+   return launch_overlapped(kern, dim3(grid), dim3(kAsyncLowWarps * 32), smem, stream, p, ag, pp);
 }
 
 }  // namespace lbm
