@@ -32,6 +32,7 @@
 
 #include "../../include/lbm_gb300.h"
 #include "lbm_f64x.cuh"
+#include "lbm_launch.cuh"
 #include "lbm_step_async.cuh"
 
 using namespace lbm;
@@ -78,6 +79,7 @@ __global__ void __launch_bounds__(kSparseThreads, sparse_min_blocks<Q>()) sparse
                                                                      const double* src, double* dst)
 {
    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+   wait_prior_grid();
    if (k >= count) return;
    const int64_t i = start + k;
    // Element indices fit 32 bits: the reference's int32 adjacency requires
@@ -154,6 +156,7 @@ __global__ void __launch_bounds__(kSparseAsyncWarps * 32, kSparseAsyncBlocks) sp
    const uint32_t nw = gridDim.x * kSparseAsyncWarps;
    uint32_t t = blockIdx.x * kSparseAsyncWarps + warp;
    if (t >= ntiles) return;
+   wait_prior_grid();
    unsigned long long* mine = sparse_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 8;
@@ -245,9 +248,8 @@ cudaError_t launch_sparse_async(const KParams& p, const int32_t* adj, int64_t nf
    const uint32_t ntiles = (uint32_t)((count + 31) / 32);
    const uint32_t need = (ntiles + kSparseAsyncWarps - 1) / kSparseAsyncWarps;
    const unsigned grid = (unsigned)(need < (uint32_t)cached ? need : (uint32_t)cached);
-   kern<<<grid, kSparseAsyncWarps * 32, smem, stream>>>(p, adj, (uint32_t)nfluid, (uint32_t)start, (uint32_t)count,
-                                                         ntiles, src, dst);
-   return cudaGetLastError();
+   return launch_overlapped(kern, dim3(grid), dim3(kSparseAsyncWarps * 32), smem, stream, p, adj, (uint32_t)nfluid,
+                            (uint32_t)start, (uint32_t)count, ntiles, src, dst);
 }
 
 template <int Q, int AR>
@@ -262,22 +264,21 @@ cudaError_t launch_sparse_q(int kind, const KParams& p, const int32_t* adj, int6
          default: return launch_sparse_async<Q, K_AB_PULL>(p, adj, nfluid, start, count, src, dst, stream);
       }
    }
-   const unsigned grid = (unsigned)((count + kSparseThreads - 1) / kSparseThreads);
+   const dim3 grid((unsigned)((count + kSparseThreads - 1) / kSparseThreads)), block(kSparseThreads);
    switch (kind) {
       case K_AA_EVEN:
-         sparse_step_kernel<Q, AR, K_AA_EVEN><<<grid, kSparseThreads, 0, stream>>>(p, adj, nfluid, start, count, src, dst);
-         break;
+         return launch_overlapped(sparse_step_kernel<Q, AR, K_AA_EVEN>, grid, block, 0, stream, p, adj, nfluid, start,
+                                  count, src, dst);
       case K_AA_ODD:
-         sparse_step_kernel<Q, AR, K_AA_ODD><<<grid, kSparseThreads, 0, stream>>>(p, adj, nfluid, start, count, src, dst);
-         break;
+         return launch_overlapped(sparse_step_kernel<Q, AR, K_AA_ODD>, grid, block, 0, stream, p, adj, nfluid, start,
+                                  count, src, dst);
       case K_AB_PUSH:
-         sparse_step_kernel<Q, AR, K_AB_PUSH><<<grid, kSparseThreads, 0, stream>>>(p, adj, nfluid, start, count, src, dst);
-         break;
+         return launch_overlapped(sparse_step_kernel<Q, AR, K_AB_PUSH>, grid, block, 0, stream, p, adj, nfluid, start,
+                                  count, src, dst);
       default:
-         sparse_step_kernel<Q, AR, K_AB_PULL><<<grid, kSparseThreads, 0, stream>>>(p, adj, nfluid, start, count, src, dst);
-         break;
+         return launch_overlapped(sparse_step_kernel<Q, AR, K_AB_PULL>, grid, block, 0, stream, p, adj, nfluid, start,
+                                  count, src, dst);
    }
-   return cudaGetLastError();
 }
 
 lbm_status sparse_launch(lbm_sparse_handle* h, int kind, const void* src, void* dst, int64_t start, int64_t count)
