@@ -43,6 +43,7 @@ struct lbm_handle {
    cudaEvent_t chunk_free[2] = {nullptr, nullptr};
    double* partials = nullptr;     // reduction scratch: plane partials or 4 doubles per loss block
    double* reduce_out = nullptr;   // 4 doubles
+   uint32_t* sched = nullptr;      // tile counter of the persistent step kernels (zero between launches)
    cudaStream_t stream = nullptr;
    // Compact fluid-only storage (cfg.compact): the steps run on cbuf; buf[0]
    // is the dense copy that set-up, readouts and host transfers use, brought
@@ -52,13 +53,10 @@ struct lbm_handle {
    uint64_t cbuf_bytes = 0;
    uint32_t nf32 = 0, cplane = 0, nrow_tiles = 0;
    uint32_t* dcell = nullptr;       // [nf] dense cell of each fluid cell
-   uint32_t* ctile_first = nullptr;
-   uint32_t* ctile_row = nullptr;
-   RowInfo* crows = nullptr;        // [ny nz]
-   uint16_t* cpre = nullptr;        // [ncell]
-   uint16_t* cxs = nullptr;         // [nf]
-   uint32_t* clk = nullptr;         // [nf]
-   size_t compact_meta_bytes[7] = {0, 0, 0, 0, 0, 0, 0};
+   OddTile* ctiles = nullptr;       // [nrow_tiles] row tiles of the odd step
+   uint2* cu = nullptr;             // [nrow_tiles * 32] row counts of the tile lanes
+   uint32_t* clk = nullptr;         // [nrow_tiles * 32] link words of the tile lanes
+   size_t compact_meta_bytes[4] = {0, 0, 0, 0};
    bool dense_current = true;       // buf[0] holds the latest state
    bool compact_current = false;    // cbuf holds the latest state
    std::string err;
@@ -157,6 +155,7 @@ KParams make_params(const lbm_handle* h, int64_t start, int64_t end, Launch& L)
    p.force_field_f = h->force_field_f;
    p.porosity = h->porosity;
    p.porosity_f = h->porosity_f;
+   p.sched = h->sched;
    int bx = (int)std::min<int64_t>(256, ((c.nx + 31) / 32) * 32);
    L.block = dim3(bx, 1, 1);
    L.grid = dim3((c.nx + bx - 1) / bx, c.ny, (unsigned)(z1 - z0));
@@ -308,87 +307,117 @@ void dense_written(lbm_handle* h)
 CompactGeom compact_geom(const lbm_handle* h)
 {
    CompactGeom g;
-   g.tile_first = h->ctile_first;
-   g.tile_row = h->ctile_row;
-   g.rows = h->crows;
-   g.pre = h->cpre;
-   g.xs = h->cxs;
+   g.tiles = h->ctiles;
+   g.u = h->cu;
    g.lk = h->clk;
    g.nrow_tiles = h->nrow_tiles;
    g.nf = h->nf32;
    g.cplane = h->cplane;
-   g.nx = h->cfg.nx;
-   g.ny = h->cfg.ny;
-   g.nz = h->cfg.nz;
-   g.m_ny = h->cfg.ny == 1 ? 0 : (~0ull / (uint64_t)h->cfg.ny) + 1;
    for (int k = 0; k < 27; k++) g.soff[k] = (uint32_t)k * h->cplane;
    return g;
 }
 
 void free_compact(lbm_handle* h)
 {
-   void* ptrs[7] = {h->dcell, h->ctile_first, h->ctile_row, h->crows, h->cpre, h->cxs, h->clk};
-   for (int k = 0; k < 7; k++) {
+   void* ptrs[4] = {h->dcell, h->ctiles, h->cu, h->clk};
+   for (int k = 0; k < 4; k++) {
       dev_free(h, ptrs[k], h->compact_meta_bytes[k]);
       h->compact_meta_bytes[k] = 0;
    }
-   h->dcell = h->ctile_first = h->ctile_row = h->clk = nullptr;
-   h->crows = nullptr;
-   h->cpre = h->cxs = nullptr;
+   h->dcell = h->clk = nullptr;
+   h->ctiles = nullptr;
+   h->cu = nullptr;
    dev_free(h, h->cbuf, h->cbuf_bytes);
    h->cbuf = nullptr;
    h->cbuf_bytes = 0;
 }
 
 // The compact numbering of the fluid cells (dense order, solids left out),
-// its row table, the per-cell prefix counts, the row tiles of the odd step
-// and the compact buffer, from the host mask (null: every cell fluid); the
-// link words are gathered from the dense ones.
+// the row tiles of the odd step with their lanes' row counts, and the compact
+// buffer, from the host mask (null: every cell fluid); the lanes' link words
+// are gathered from the dense ones.
 lbm_status build_compact(lbm_handle* h, const uint8_t* solid)
 {
-   const int nx = h->cfg.nx;
-   const int64_t nrows = (int64_t)h->cfg.ny * h->cfg.nz;
-   std::vector<uint32_t> dcell, tfirst, trow;
-   std::vector<RowInfo> rows((size_t)nrows);
-   std::vector<uint16_t> pre((size_t)h->ncell), xs;
+   const int nx = h->cfg.nx, ny = h->cfg.ny, nz = h->cfg.nz;
+   const int64_t nrows = (int64_t)ny * nz;
+   // per row: first compact index and fluid count; per cell: fluid cells
+   // before it in its row
+   std::vector<uint32_t> dcell, rstart((size_t)nrows), rcount((size_t)nrows);
+   std::vector<uint16_t> pre((size_t)h->ncell);
    dcell.reserve((size_t)h->nfluid);
-   xs.reserve((size_t)h->nfluid);
    for (int64_t r = 0; r < nrows; r++) {
-      const uint32_t start = (uint32_t)dcell.size();
+      rstart[(size_t)r] = (uint32_t)dcell.size();
       uint32_t cnt = 0;
       for (int x = 0; x < nx; x++) {
          const int64_t c = r * nx + x;
          pre[(size_t)c] = (uint16_t)cnt;
          if (!solid || !solid[c]) {
             dcell.push_back((uint32_t)c);
-            xs.push_back((uint16_t)x);
             cnt++;
          }
       }
-      rows[(size_t)r] = {start, cnt};
-      for (uint32_t k = 0; k < cnt; k += 32) {
-         tfirst.push_back(start + k);
-         trow.push_back((uint32_t)r);
+      rcount[(size_t)r] = cnt;
+   }
+   // row tiles: up to 32 consecutive fluid cells of a row within 255 of the
+   // first one's x, so the per-lane counts fit a byte
+   std::vector<OddTile> tiles;
+   std::vector<uint2> ucounts;
+   tiles.reserve(dcell.size() / 32 + (size_t)nrows);
+   ucounts.reserve(dcell.size() + (size_t)nrows * 32);
+   for (int64_t r = 0; r < nrows; r++) {
+      const int y = (int)(r % ny), z = (int)(r / ny);
+      int64_t nbr[9];
+      for (int k = 0; k < 9; k++) {
+         const int yy = (y + k / 3 - 1 + ny) % ny, zz = (z + k % 3 - 1 + nz) % nz;
+         nbr[k] = (int64_t)yy + (int64_t)ny * zz;
+      }
+      const uint32_t start = rstart[(size_t)r], cnt = rcount[(size_t)r];
+      uint32_t q = 0;
+      while (q < cnt) {
+         const int xa = (int)(dcell[start + q] - (uint32_t)(r * nx));
+         OddTile t{};
+         for (int k = 0; k < 9; k++) {
+            const int64_t rk = nbr[k];
+            t.b[k] = rstart[(size_t)rk] + pre[(size_t)(rk * nx + xa)];
+            t.n[k] = rcount[(size_t)rk];
+         }
+         uint32_t m = 0;
+         while (m < 32 && q + m < cnt) {
+            const int x = (int)(dcell[start + q + m] - (uint32_t)(r * nx));
+            if (x - xa > 255) break;
+            uint32_t w[2] = {0u, 0u};
+            int byte = 0;
+            for (int k = 0; k < 9; k++) {
+               if (k == 4) continue;
+               const int64_t rk = nbr[k];
+               const uint32_t uk = (uint32_t)pre[(size_t)(rk * nx + x)] - pre[(size_t)(rk * nx + xa)];
+               w[byte / 4] |= uk << (8 * (byte % 4));
+               byte++;
+            }
+            ucounts.push_back(make_uint2(w[0], w[1]));
+            m++;
+         }
+         t.ncell = m;
+         for (uint32_t l = m; l < 32; l++) ucounts.push_back(make_uint2(0u, 0u));
+         tiles.push_back(t);
+         q += m;
       }
    }
    free_compact(h);
    h->nf32 = (uint32_t)dcell.size();
    h->cplane = (h->nf32 + 255u) / 256u * 256u;
-   h->nrow_tiles = (uint32_t)tfirst.size();
-   if ((uint64_t)h->Q * h->cplane >= (1ull << 32))
+   if ((uint64_t)h->Q * h->cplane >= (1ull << 32) || tiles.size() >= (1u << 27))
       return fail(h, LBM_ERR_UNSUPPORTED, "compact storage needs Q * fluid cells below 2^32");
+   h->nrow_tiles = (uint32_t)tiles.size();
    struct Part {
       void** dst;
       const void* src;
       size_t bytes;
-   } parts[7] = {{(void**)&h->dcell, dcell.data(), 4 * dcell.size()},
-                 {(void**)&h->ctile_first, tfirst.data(), 4 * tfirst.size()},
-                 {(void**)&h->ctile_row, trow.data(), 4 * trow.size()},
-                 {(void**)&h->crows, rows.data(), sizeof(RowInfo) * rows.size()},
-                 {(void**)&h->cpre, pre.data(), 2 * pre.size()},
-                 {(void**)&h->cxs, xs.data(), 2 * xs.size()},
-                 {(void**)&h->clk, nullptr, 4 * dcell.size()}};
-   for (int k = 0; k < 7; k++) {
+   } parts[4] = {{(void**)&h->dcell, dcell.data(), 4 * dcell.size()},
+                 {(void**)&h->ctiles, tiles.data(), sizeof(OddTile) * tiles.size()},
+                 {(void**)&h->cu, ucounts.data(), sizeof(uint2) * ucounts.size()},
+                 {(void**)&h->clk, nullptr, 4 * ucounts.size()}};
+   for (int k = 0; k < 4; k++) {
       const size_t bytes = std::max<size_t>(parts[k].bytes, 16);
       lbm_status st = dev_alloc(h, parts[k].dst, bytes);
       if (st != LBM_OK) return st;
@@ -396,7 +425,7 @@ lbm_status build_compact(lbm_handle* h, const uint8_t* solid)
       if (parts[k].src && parts[k].bytes)
          LBM_CUDA(h, cudaMemcpyAsync(*parts[k].dst, parts[k].src, parts[k].bytes, cudaMemcpyHostToDevice, h->stream));
    }
-   LBM_CUDA(h, launch_compact_links(h->dcell, h->links, h->clk, h->nf32, h->stream));
+   LBM_CUDA(h, launch_compact_links(h->ctiles, h->nrow_tiles, h->dcell, h->links, nx, h->clk, h->stream));
    h->cbuf_bytes = std::max<uint64_t>((uint64_t)h->cplane * h->Q * h->elem, 16);
    lbm_status st = dev_alloc(h, &h->cbuf, h->cbuf_bytes);
    if (st != LBM_OK) return st;
@@ -473,13 +502,11 @@ void lbm_destroy(lbm_handle* h)
    }
    cudaFree(h->partials);
    cudaFree(h->reduce_out);
+   cudaFree(h->sched);
    cudaFree(h->cbuf);
    cudaFree(h->dcell);
-   cudaFree(h->ctile_first);
-   cudaFree(h->ctile_row);
-   cudaFree(h->crows);
-   cudaFree(h->cpre);
-   cudaFree(h->cxs);
+   cudaFree(h->ctiles);
+   cudaFree(h->cu);
    cudaFree(h->clk);
    if (prev >= 0) cudaSetDevice(prev);
    delete h;
@@ -554,6 +581,11 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_handle** out)
       st = dev_alloc(h, (void**)&h->partials, plane_bytes > loss_bytes ? plane_bytes : loss_bytes);
    }
    if (st == LBM_OK) st = dev_alloc(h, (void**)&h->reduce_out, sizeof(double) * 4);
+   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->sched, 16);
+   if (st == LBM_OK) {
+      const cudaError_t e = cudaMemset(h->sched, 0, 16);
+      if (e != cudaSuccess) st = cuda_fail(h, e, "cudaMemset");
+   }
    if (st == LBM_OK) st = lbm_set_solid(h, nullptr);
    if (st == LBM_OK) st = lbm_init_equilibrium(h, nullptr, nullptr);
    if (st != LBM_OK) {

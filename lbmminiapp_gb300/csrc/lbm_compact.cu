@@ -68,14 +68,32 @@ template <> struct PairWord<__nv_bfloat16> {
    }
 };
 
+// Per warp, the odd step's pipeline: while tile j collides, tile j + 1's
+// populations and tile j + 2's metadata are copied: two population stages and
+// three metadata slots, each slot the tile record, the lanes' row counts and
+// the lanes' link words.
+constexpr uint32_t kOddStages = 2;
+constexpr uint32_t kMetaSlots = 3;
+constexpr uint32_t kMetaTile = 0;                         // OddTile, 20 words
+constexpr uint32_t kMetaU = 20;                           // uint2 per lane
+constexpr uint32_t kMetaLk = kMetaU + 2 * 32;             // uint32 per lane
+constexpr uint32_t kMetaWords = kMetaLk + 32;             // 116 words, 464 bytes
+static_assert(kMetaWords % 4 == 0, "metadata slots stay 16-byte aligned");
+
+// Words of shared memory per warp of the odd step: the population stages
+// (one word per lane and direction) and the metadata slots.
+template <int Q>
+constexpr uint32_t odd_warp_words() { return kOddStages * Q * 32 + kMetaSlots * kMetaWords; }
+
 // Shared memory per block: a two-stage buffer per warp of one word per lane
-// and direction (the even step's words hold two cells).
+// and direction (the even step's words hold two cells), and the odd step's
+// metadata slots.
 template <int Q, int ST, int KIND>
 constexpr size_t compact_smem_bytes()
 {
    using T = typename Store<ST>::T;
-   return (size_t)kCompactWarps * kAsyncStages * Q * 32 *
-          (KIND == K_AA_EVEN ? sizeof(typename PairWord<T>::W) : sizeof(uint32_t));
+   return KIND == K_AA_EVEN ? (size_t)kCompactWarps * kAsyncStages * Q * 32 * sizeof(typename PairWord<T>::W)
+                            : (size_t)kCompactWarps * odd_warp_words<Q>() * sizeof(uint32_t);
 }
 
 // Address of the aligned 4-byte word holding element e (the element itself
@@ -87,14 +105,6 @@ __device__ __forceinline__ const void* word_of(const T* base, uint32_t e)
       return reinterpret_cast<const void*>(reinterpret_cast<uintptr_t>(base + e) & ~(uintptr_t)3);
    else
       return base + e;
-}
-
-// Direction index of the velocity (cx, cy, cz), -1 if the lattice has none.
-__host__ __device__ constexpr int dir_of(int Q, int cx, int cy, int cz)
-{
-   for (int s = 0; s < Q; s++)
-      if (lat_c(Q, s, 0) == cx && lat_c(Q, s, 1) == cy && lat_c(Q, s, 2) == cz) return s;
-   return -1;
 }
 
 template <int Q, int ST, bool FORCE>
@@ -121,8 +131,6 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_even_kernel(con
    const int warp = threadIdx.x >> 5;
    const uint32_t ntiles = (g.nf + 63) / 64;
    const uint32_t nw = gridDim.x * kCompactWarps;
-   uint32_t t = blockIdx.x * kCompactWarps + warp;
-   if (t >= ntiles) return;
    wait_prior_grid();
    W* mine = reinterpret_cast<W*>(compact_smem) + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
@@ -138,102 +146,143 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_even_kernel(con
          else cp_async4(dst, src);
       }
    };
-   issue(t, sbase);
-   cp_async_commit();
-   int stage = 0;
-   for (;;) {
-      const uint32_t next = t + nw;
-      if (next < ntiles) issue(next, sbase + (stage ^ 1) * kStageBytes);
+   // tiles: two per warp in a fixed order, then the launch's tile feed
+   TileFeed feed = feed_start(p.sched, 2u * nw, ntiles, lane);
+   uint32_t t = blockIdx.x * kCompactWarps + warp;
+   if (t < ntiles) {
+      uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
+      issue(t, sbase);
       cp_async_commit();
-      cp_async_wait_prev();
-      const uint32_t i0 = t * 64 + 2 * (uint32_t)lane;
-      if (i0 < g.nf) {
-         const W* sm = mine + stage * Q * 32;
-         float G0[Q], G1[Q];
+      int stage = 0;
+      for (;;) {
+         if (t1 < ntiles) issue(t1, sbase + (stage ^ 1) * kStageBytes);
+         cp_async_commit();
+         cp_async_wait_prev();
+         const uint32_t i0 = t * 64 + 2 * (uint32_t)lane;
+         if (i0 < g.nf) {
+            const W* sm = mine + stage * Q * 32;
+            float G0[Q], G1[Q];
 #pragma unroll
-         for (int s = 0; s < Q; s++) PW::unpack(sm[s * 32 + lane], G0[s], G1[s]);
-         auto emit = [&](int s, float a, float b) {
-            *reinterpret_cast<W*>(buf + (g.soff[s] + i0)) = PW::pack(a, b);
-         };
-         collide2_f32_emit<Q, ST, FORCE>(G0, G1, p, emit);
+            for (int s = 0; s < Q; s++) PW::unpack(sm[s * 32 + lane], G0[s], G1[s]);
+            auto emit = [&](int s, float a, float b) {
+               *reinterpret_cast<W*>(buf + (g.soff[s] + i0)) = PW::pack(a, b);
+            };
+            collide2_f32_emit<Q, ST, FORCE>(G0, G1, p, emit);
+         }
+         if (t1 >= ntiles) break;
+         t = t1;
+         t1 = feed_next(feed, p.sched, 2u * nw, ntiles, lane);
+         stage ^= 1;
       }
-      if (next >= ntiles) break;
-      t = next;
-      stage ^= 1;
    }
+   feed_done(p.sched);
 }
 
 // ------------------------------------------------------------------ odd
-// Lane state of a row tile.  base[k] is the compact index of (x, row k) as
-// if that cell were fluid, rows k = 3 (dy + 1) + (dz + 1); n[k] is the row's
-// fluid count, used for the periodic wrap of x at the row ends.
-struct OddLane {
+__device__ __forceinline__ void cp_async16(uint32_t smem, const void* g)
+{
+   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// Copies tile t's metadata into a slot (sm: its shared-memory address).
+__device__ __forceinline__ void odd_meta_issue(const CompactGeom& g, uint32_t t, int lane, uint32_t sm)
+{
+   if (lane < 5) cp_async16(sm + 4u * kMetaTile + 16u * lane, reinterpret_cast<const uint4*>(g.tiles + t) + lane);
+   const uint32_t tl = t * 32u + (uint32_t)lane;
+   cp_async8(sm + 4u * kMetaU + 8u * lane, g.u + tl);
+   cp_async4(sm + 4u * kMetaLk + 4u * lane, g.lk + tl);
+}
+
+// A lane's view of its tile: its cell i, link word, and the compact index of
+// the fluid cell at x (N), one below (Nm: at x - 1) and one past (Np: at x + 1)
+// in each row k, valid where that neighbour is fluid.
+template <int Q>
+struct OddView {
    uint32_t i, lk;
-   bool active, x0, xl;   // x0: x == 0; xl: x == nx - 1
-   uint32_t base[9];
-   uint32_t n[9];
+   uint32_t N[9], Nm[9], Np[9];
 };
 
-__device__ __forceinline__ int wrap(int v, int n) { return v < 0 ? v + n : (v >= n ? v - n : v); }
-
-__device__ __forceinline__ void odd_prepare(const CompactGeom& g, uint32_t row, uint32_t first, int lane,
-                                            OddLane& L)
+// Direction index of the velocity (cx, cy, cz), -1 if the lattice has none.
+__host__ __device__ constexpr int dir_of(int Q, int cx, int cy, int cz)
 {
-   const RowInfo own = g.rows[row];
-   L.i = first + (uint32_t)lane;
-   L.active = L.i < own.start + own.count;
-   const uint32_t ii = L.active ? L.i : first;
-   const int x = (int)__ldg(g.xs + ii);
-   L.lk = __ldg(g.lk + ii);
-   L.x0 = x == 0;
-   L.xl = x == g.nx - 1;
-   const uint32_t z = div_magic(row, (uint32_t)g.ny, g.m_ny);
-   const int y = (int)(row - z * (uint32_t)g.ny);
+   for (int s = 0; s < Q; s++)
+      if (lat_c(Q, s, 0) == cx && lat_c(Q, s, 1) == cy && lat_c(Q, s, 2) == cz) return s;
+   return -1;
+}
+
+template <int Q>
+__device__ __forceinline__ void odd_view(const uint32_t* m, int lane, OddView<Q>& v)
+{
+   v.lk = m[kMetaLk + lane];
+   const uint2 u = *reinterpret_cast<const uint2*>(m + kMetaU + 2 * lane);
+   const uint4 b0 = *reinterpret_cast<const uint4*>(m + kMetaTile);
+   const uint4 b1 = *reinterpret_cast<const uint4*>(m + kMetaTile + 4);
+   const uint32_t b[9] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w, m[kMetaTile + 8]};
+   v.i = b[4] + (uint32_t)lane;
 #pragma unroll
    for (int k = 0; k < 9; k++) {
       if (k == 4) {
-         L.base[4] = L.i;
-         L.n[4] = own.count;
+         v.N[4] = v.i;
+         v.Nm[4] = v.i - 1u;
+         v.Np[4] = v.i + 1u;
          continue;
       }
-      const int dy = k / 3 - 1, dz = k % 3 - 1;
-      const uint32_t r2 = (uint32_t)wrap(y + dy, g.ny) + (uint32_t)g.ny * (uint32_t)wrap((int)z + dz, g.nz);
-      const RowInfo ri = g.rows[r2];
-      L.base[k] = ri.start + (uint32_t)__ldg(g.pre + (r2 * (uint32_t)g.nx + (uint32_t)x));
-      L.n[k] = ri.count;
+      const int byte = k < 4 ? k : k - 1;
+      const uint32_t w = byte < 4 ? u.x : u.y;
+      v.N[k] = b[k] + __byte_perm(w, 0u, 0x4440u | (uint32_t)(byte & 3));
+      v.Nm[k] = v.N[k] - 1u;
+      // one past (x, row k) when that cell is fluid: the link bit of (0, dy, dz)
+      v.Np[k] = v.N[k] + (((v.lk >> dir_of(Q, 0, k / 3 - 1, k % 3 - 1)) & 1u) ^ 1u);
+   }
+   if (v.lk & (kRowStartBit | kRowEndBit)) {
+      // a row end: the periodic wrap of x
+      const uint32_t* n = m + kMetaTile + 9;
+#pragma unroll
+      for (int k = 0; k < 9; k++) {
+         if (v.lk & kRowStartBit) v.Nm[k] += n[k];
+         if (v.lk & kRowEndBit) v.Np[k] -= n[k];
+      }
    }
 }
 
-// Compact index of the fluid neighbour at x + (dx, dy, dz).
+// Element of the fluid neighbour at x + (dx, dy, dz), slot offset excluded.
 template <int Q>
-__device__ __forceinline__ uint32_t nbr_index(const OddLane& L, int dx, int dy, int dz)
+__device__ __forceinline__ uint32_t odd_nbr(const OddView<Q>& v, int dx, int dy, int dz)
 {
    const int k = (dy + 1) * 3 + (dz + 1);
-   if (dx == 0) return L.base[k];
-   if (dx < 0) return L.base[k] - 1u + (L.x0 ? L.n[k] : 0u);
-   // x + 1: one past (x, row k) when that cell is fluid
-   const uint32_t fl = k == 4 ? 1u : (((L.lk >> dir_of(Q, 0, dy, dz)) & 1u) ^ 1u);
-   return L.base[k] + fl - (L.xl ? L.n[k] : 0u);
+   return dx == 0 ? v.N[k] : (dx < 0 ? v.Nm[k] : v.Np[k]);
 }
 
+// Element e_s read for direction opp(s) and written for direction s: slot
+// opp(s) of the neighbour at x + c_s, own slot s when that neighbour is
+// blocked (and for the rest direction).
+template <int Q>
+__device__ __forceinline__ uint32_t odd_elem(const CompactGeom& g, const OddView<Q>& v, int s)
+{
+   if (s == lat_rest(Q) || ((v.lk >> s) & 1u)) return g.soff[s] + v.i;
+   return g.soff[lat_opp(Q, s)] + odd_nbr<Q>(v, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
+}
+
+// Copies the lane's populations (direction s from e_opp(s)); returns the
+// word-half mask.
 template <int Q, typename T>
-__device__ __forceinline__ uint32_t odd_issue(const T* buf, const CompactGeom& g, const OddLane& L, int lane,
-                                              uint32_t sb)
+__device__ __forceinline__ uint32_t odd_pop_issue(const T* buf, const CompactGeom& g, const OddView<Q>& v, int lane,
+                                                  uint32_t sb)
 {
    uint32_t halves = 0u;
-   if (!L.active) return halves;
 #pragma unroll
    for (int s = 0; s < Q; s++) {
-      const int o = lat_opp(Q, s);
-      uint32_t e;
-      if (s == lat_rest(Q) || ((L.lk >> o) & 1u)) e = g.soff[s == lat_rest(Q) ? s : o] + L.i;
-      else e = g.soff[s] + nbr_index<Q>(L, -lat_c(Q, s, 0), -lat_c(Q, s, 1), -lat_c(Q, s, 2));
+      const uint32_t e = odd_elem<Q>(g, v, lat_opp(Q, s));
       cp_async4(sb + (uint32_t)(s * 32 + lane) * 4u, word_of(buf, e));
       if constexpr (sizeof(T) == 2) halves |= (e & 1u) << s;
    }
    return halves;
 }
 
+// Tiles come from the launch's tile feed (lbm_launch.cuh): three per warp in
+// a fixed order, the rest as the warps ask for them (tiles differ in cost:
+// bounce-back, partial tiles).
 template <int Q, int ST, bool FORCE>
 __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(const KParams p, const CompactGeom g,
                                                                             typename Store<ST>::T* buf)
@@ -243,57 +292,68 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(cons
    const int warp = threadIdx.x >> 5;
    const uint32_t ntiles = g.nrow_tiles;
    const uint32_t nw = gridDim.x * kCompactWarps;
-   uint32_t t = blockIdx.x * kCompactWarps + warp;
-   if (t >= ntiles) return;
    wait_prior_grid();
-   uint32_t* mine = compact_smem + (size_t)warp * kAsyncStages * Q * 32;
-   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
+   uint32_t* pop = compact_smem + (size_t)warp * odd_warp_words<Q>();
+   uint32_t* meta = pop + kOddStages * Q * 32;
+   const uint32_t pop_s = (uint32_t)__cvta_generic_to_shared(pop);
+   const uint32_t meta_s = (uint32_t)__cvta_generic_to_shared(meta);
    constexpr uint32_t kStageBytes = Q * 32 * 4;
-   OddLane cur;
-   odd_prepare(g, __ldg(g.tile_row + t), __ldg(g.tile_first + t), lane, cur);
-   uint32_t halves = odd_issue<Q>(buf, g, cur, lane, sbase);
-   cp_async_commit();
-   // the tile table one tile ahead of the prefetch
-   uint32_t row_ahead = 0u, first_ahead = 0u;
-   if (t + nw < ntiles) {
-      row_ahead = __ldg(g.tile_row + t + nw);
-      first_ahead = __ldg(g.tile_first + t + nw);
-   }
-   int stage = 0;
-   for (;;) {
-      const uint32_t next = t + nw;
-      OddLane nxt = cur;
-      uint32_t halves_next = 0u;
-      if (next < ntiles) {
-         odd_prepare(g, row_ahead, first_ahead, lane, nxt);
-         if (next + nw < ntiles) {
-            row_ahead = __ldg(g.tile_row + next + nw);
-            first_ahead = __ldg(g.tile_first + next + nw);
-         }
-         halves_next = odd_issue<Q>(buf, g, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
+   constexpr uint32_t kSlotBytes = kMetaWords * 4;
+   TileFeed feed = feed_start(p.sched, 3u * nw, ntiles, lane);
+   uint32_t t = blockIdx.x * kCompactWarps + warp;
+   if (t < ntiles) {
+      uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
+      uint32_t t2 = t + 2u * nw < ntiles ? t + 2u * nw : ntiles;
+      odd_meta_issue(g, t, lane, meta_s);
+      if (t1 < ntiles) odd_meta_issue(g, t1, lane, meta_s + kSlotBytes);
+      cp_async_commit();
+      cp_async_wait_all();
+      __syncwarp();
+      uint32_t halves = 0u;
+      {
+         OddView<Q> v;
+         odd_view<Q>(meta, lane, v);
+         if (!(v.lk & kSolidBit)) halves = odd_pop_issue<Q>(buf, g, v, lane, pop_s);
       }
       cp_async_commit();
-      cp_async_wait_prev();
-      if (cur.active) {
-         const uint32_t* sm = mine + stage * Q * 32;
-         float G[Q], o[Q];
-#pragma unroll
-         for (int s = 0; s < Q; s++) G[s] = word_value<ST>(sm[s * 32 + lane], (halves >> s) & 1u);
-         collide_cell<Q, ST, FORCE>(G, o, p);
-#pragma unroll
-         for (int s = 0; s < Q; s++) {
-            uint32_t e;
-            if (s == lat_rest(Q) || ((cur.lk >> s) & 1u)) e = g.soff[s] + cur.i;
-            else e = g.soff[lat_opp(Q, s)] + nbr_index<Q>(cur, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2));
-            store_raw(buf + e, o[s]);
+      uint32_t slot = 0, stage = 0;
+      for (;;) {
+         const uint32_t slot1 = slot == 2 ? 0 : slot + 1, slot2 = slot1 == 2 ? 0 : slot1 + 1;
+         const uint32_t t3 = t2 < ntiles ? feed_next(feed, p.sched, 3u * nw, ntiles, lane) : ntiles;
+         // this tile's populations and the next tile's metadata have landed
+         cp_async_wait_all();
+         __syncwarp();
+         if (t2 < ntiles) odd_meta_issue(g, t2, lane, meta_s + slot2 * kSlotBytes);
+         uint32_t halves_next = 0u;
+         if (t1 < ntiles) {
+            OddView<Q> v;
+            odd_view<Q>(meta + slot1 * kMetaWords, lane, v);
+            if (!(v.lk & kSolidBit))
+               halves_next = odd_pop_issue<Q>(buf, g, v, lane, pop_s + (stage ^ 1u) * kStageBytes);
          }
+         cp_async_commit();
+         const uint32_t* m = meta + slot * kMetaWords;
+         if (!(m[kMetaLk + lane] & kSolidBit)) {
+            const uint32_t* sm = pop + stage * Q * 32;
+            float G[Q], o[Q];
+#pragma unroll
+            for (int s = 0; s < Q; s++) G[s] = word_value<ST>(sm[s * 32 + lane], (halves >> s) & 1u);
+            collide_cell<Q, ST, FORCE>(G, o, p);
+            OddView<Q> v;
+            odd_view<Q>(m, lane, v);
+#pragma unroll
+            for (int s = 0; s < Q; s++) store_raw(buf + odd_elem<Q>(g, v, s), o[s]);
+         }
+         if (t1 >= ntiles) break;
+         t = t1;
+         t1 = t2;
+         t2 = t3;
+         halves = halves_next;
+         slot = slot1;
+         stage ^= 1u;
       }
-      if (next >= ntiles) break;
-      t = next;
-      cur = nxt;
-      halves = halves_next;
-      stage ^= 1;
    }
+   feed_done(p.sched);
 }
 
 // Persistent grid: as many blocks as fit on the device at once, queried once
@@ -379,10 +439,20 @@ __global__ void compress_kernel(const uint32_t* dcell, uint32_t nf, uint32_t cpl
    for (int s = 0; s < Q; s++) cbuf[(uint64_t)s * cplane + i] = dense[(int64_t)s * plane + c];
 }
 
-__global__ void gather_links_kernel(const uint32_t* dcell, const uint32_t* links, uint32_t* lk, uint32_t nf)
+__global__ void gather_links_kernel(const OddTile* tiles, uint32_t ntiles, const uint32_t* dcell,
+                                    const uint32_t* links, int nx, uint32_t* lk)
 {
-   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-   if (i < nf) lk[i] = links ? links[dcell[i]] : 0u;
+   const uint64_t tl = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+   if (tl >= (uint64_t)ntiles * 32u) return;
+   const OddTile& tile = tiles[tl / 32u];
+   const uint32_t lane = (uint32_t)(tl % 32u);
+   uint32_t w = kSolidBit;
+   if (lane < tile.ncell) {
+      const uint32_t c = dcell[tile.b[4] + lane];
+      const uint32_t x = c % (uint32_t)nx;
+      w = (links ? links[c] : 0u) | (x == 0u ? kRowStartBit : 0u) | (x == (uint32_t)nx - 1u ? kRowEndBit : 0u);
+   }
+   lk[tl] = w;
 }
 
 unsigned blocks_of(uint32_t n) { return (n + 255) / 256; }
@@ -436,11 +506,12 @@ cudaError_t launch_compact_compress(int Q, int storage, const uint32_t* dcell, u
    return cudaGetLastError();
 }
 
-cudaError_t launch_compact_links(const uint32_t* dcell, const uint32_t* links, uint32_t* lk, uint32_t nf,
-                                 cudaStream_t stream)
+cudaError_t launch_compact_links(const OddTile* tiles, uint32_t ntiles, const uint32_t* dcell,
+                                 const uint32_t* links, int nx, uint32_t* lk, cudaStream_t stream)
 {
-   if (nf == 0) return cudaSuccess;
-   gather_links_kernel<<<blocks_of(nf), 256, 0, stream>>>(dcell, links, lk, nf);
+   if (ntiles == 0) return cudaSuccess;
+   if (ntiles >= (1u << 27)) return cudaErrorInvalidValue;
+   gather_links_kernel<<<blocks_of(ntiles * 32u), 256, 0, stream>>>(tiles, ntiles, dcell, links, nx, lk);
    return cudaGetLastError();
 }
 

@@ -3,18 +3,21 @@
 // dense grid's order (x fastest, then y, then z) with the solid cells left
 // out, direction s of fluid cell i at s * cplane + i.
 //
-// Streaming needs no per-direction adjacency list.  A row r = y + ny z holds
-// its fluid cells at consecutive indices from rows[r].start, and pre[c] counts
-// the fluid cells of c's row that lie before c; so the fluid cell at (x', r')
-// is rows[r'].start + pre[x' + nx r'].  A lane of row r at x needs, for each
-// of the 9 rows r' = r + (dy, dz), one value base = rows[r'].start +
-// pre[x + nx r'] (its own row: its own index i); the neighbours at x - 1,
-// x and x + 1 of that row are base - 1, base and base + [x fluid in r'], with
-// the periodic wrap of x folded in through the row's fluid count.  Whether a
-// neighbour is fluid comes from the cell's link word, as in the dense layout
-// (bit s set: the neighbour at x + c_s is solid or outside a non-periodic
-// face).  This costs 2 bytes per dense cell (pre) and 6 per fluid cell (x and
-// the link word), against the 4 Q bytes per fluid cell of an adjacency list.
+// Streaming needs no per-direction adjacency list.  The odd step works on
+// row tiles: up to 32 consecutive fluid cells of one row r = y + ny z whose x
+// lie within 256 of the tile's first x (xa).  Per tile, for each of the 9 rows
+// r' = r + (dy, dz) (periodic wrap of y and z), b[k] is the compact index of
+// the first fluid cell of r' at or after xa and n[k] the fluid count of r';
+// per cell, u[k] counts the fluid cells of r' in [xa, x).  The fluid cell at
+// (x, r') is then b[k] + u[k], its neighbours at x - 1 and x + 1 are one below
+// and one past it (past it only when (x, r') is fluid), and at the row ends
+// the periodic wrap of x adds or takes off n[k].  Whether a neighbour is fluid
+// comes from the cell's link word, as in the dense layout (bit s set: the
+// neighbour at x + c_s is solid or outside a non-periodic face).  This costs
+// 80 bytes per tile and 12 per cell (the 8 counts u[k] of the other rows and
+// the link word), against the 4 Q bytes per fluid cell of an adjacency list,
+// and every one of it is read with the cell's own index: no load of the odd
+// step depends on another.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -25,23 +28,27 @@
 
 namespace lbm {
 
-struct RowInfo {
-   uint32_t start;   // compact index of the row's first fluid cell
-   uint32_t count;   // fluid cells in the row
+// Row tile of the odd step, 80 bytes (five 16-byte copies).
+struct OddTile {
+   uint32_t b[9];       // compact index of the first fluid cell at or after xa in row k = 3 (dy + 1) + (dz + 1)
+   uint32_t n[9];       // fluid cells in row k
+   uint32_t ncell;      // fluid cells in the tile (1..32)
+   uint32_t pad;
 };
+static_assert(sizeof(OddTile) == 80, "OddTile is five 16-byte words");
+
+// Link-word bits of a compact cell beyond the direction bits (Q <= 27) and
+// kSolidBit (a tile lane without a cell): the cell sits at x = 0 / x = nx - 1.
+constexpr uint32_t kRowStartBit = 1u << 29;
+constexpr uint32_t kRowEndBit = 1u << 30;
 
 struct CompactGeom {
-   const uint32_t* tile_first;   // [nrow_tiles] first compact index of a row tile (up to 32 cells of one row)
-   const uint32_t* tile_row;     // [nrow_tiles] its row y + ny z
-   const RowInfo* rows;          // [ny nz]
-   const uint16_t* pre;          // [ncell] fluid cells before x in the cell's row
-   const uint16_t* xs;           // [nf] x of each fluid cell
-   const uint32_t* lk;           // [nf] link word of each fluid cell
+   const OddTile* tiles;         // [nrow_tiles]
+   const uint2* u;               // [nrow_tiles * 32] bytes u[k] of rows k = 0..3, 5..8 per tile lane
+   const uint32_t* lk;           // [nrow_tiles * 32] link word of each tile lane (kSolidBit: no cell)
    uint32_t nrow_tiles;
    uint32_t nf;                  // fluid cells
    uint32_t cplane;              // elements between direction planes (even, at least nf)
-   int nx, ny, nz;
-   uint64_t m_ny;                // ceil(2^64 / ny), 0 for ny = 1: row -> (y, z) by multiply-high
    uint32_t soff[27];            // s * cplane: slot offsets in the parameter bank
 };
 
@@ -55,8 +62,10 @@ cudaError_t launch_compact_expand(int Q, int storage, const uint32_t* dcell, uin
                                   const void* cbuf, void* dense, int64_t plane, cudaStream_t stream);
 cudaError_t launch_compact_compress(int Q, int storage, const uint32_t* dcell, uint32_t nf, uint32_t cplane,
                                     const void* dense, int64_t plane, void* cbuf, cudaStream_t stream);
-// lk[i] = links[dcell[i]]
-cudaError_t launch_compact_links(const uint32_t* dcell, const uint32_t* links, uint32_t* lk, uint32_t nf,
-                                 cudaStream_t stream);
+// Link words of the tile lanes: links[dcell[i]] (0 without links) with the
+// row-end bits for the cell i of each lane, kSolidBit for a lane past its
+// tile's cells.
+cudaError_t launch_compact_links(const OddTile* tiles, uint32_t ntiles, const uint32_t* dcell,
+                                 const uint32_t* links, int nx, uint32_t* lk, cudaStream_t stream);
 
 }  // namespace lbm

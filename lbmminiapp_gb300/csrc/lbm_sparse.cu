@@ -154,8 +154,6 @@ __global__ void __launch_bounds__(kSparseAsyncWarps * 32, kSparseAsyncBlocks) sp
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
    const uint32_t nw = gridDim.x * kSparseAsyncWarps;
-   uint32_t t = blockIdx.x * kSparseAsyncWarps + warp;
-   if (t >= ntiles) return;
    wait_prior_grid();
    unsigned long long* mine = sparse_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
@@ -187,36 +185,44 @@ __global__ void __launch_bounds__(kSparseAsyncWarps * 32, kSparseAsyncBlocks) sp
          cp_async8(sb + (uint32_t)(s * 32 + lane) * 8u, s64 + r);
       }
    };
-   if (sparse_gathers<KIND>()) load_ahead(t);
-   issue(t, sbase);
-   cp_async_commit();
-   if (sparse_gathers<KIND>() && t + nw < ntiles) load_ahead(t + nw);
-   int stage = 0;
-   for (;;) {
-      const uint32_t next = t + nw;
-      if (next < ntiles) {
-         issue(next, sbase + (stage ^ 1) * kStageBytes);
-         if (sparse_gathers<KIND>() && next + nw < ntiles) load_ahead(next + nw);
-      }
+   // tiles in a fixed round-robin: t is collided while t1's populations are
+   // in flight and t2's read locations are loaded
+   uint32_t t = blockIdx.x * kSparseAsyncWarps + warp;
+   if (t < ntiles) {
+      uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
+      uint32_t t2 = t + 2u * nw < ntiles ? t + 2u * nw : ntiles;
+      if (sparse_gathers<KIND>()) load_ahead(t);
+      issue(t, sbase);
       cp_async_commit();
-      cp_async_wait_prev();
-      bool act;
-      const uint32_t i = point(t, act);
-      if (act) {
-         uint32_t wl[Q];
-         if (sparse_scatters<KIND>()) {
-#pragma unroll
-            for (int s = 0; s < Q; s++) {
-               const int r = KIND == K_AA_ODD ? lat_opp(Q, s) : s;
-               wl[s] = (uint32_t)__ldg(adj + (size_t)nf * r + i);
-            }
+      if (sparse_gathers<KIND>() && t1 < ntiles) load_ahead(t1);
+      int stage = 0;
+      for (;;) {
+         if (t1 < ntiles) {
+            issue(t1, sbase + (stage ^ 1) * kStageBytes);
+            if (sparse_gathers<KIND>() && t2 < ntiles) load_ahead(t2);
          }
-         const SparseEmit<Q, KIND> emit{dst, nf, i, wl};
-         collide_f64x_shared_emit<Q>(mine + stage * Q * 32 + lane, p, emit);
+         cp_async_commit();
+         cp_async_wait_prev();
+         bool act;
+         const uint32_t i = point(t, act);
+         if (act) {
+            uint32_t wl[Q];
+            if (sparse_scatters<KIND>()) {
+#pragma unroll
+               for (int s = 0; s < Q; s++) {
+                  const int r = KIND == K_AA_ODD ? lat_opp(Q, s) : s;
+                  wl[s] = (uint32_t)__ldg(adj + (size_t)nf * r + i);
+               }
+            }
+            const SparseEmit<Q, KIND> emit{dst, nf, i, wl};
+            collide_f64x_shared_emit<Q>(mine + stage * Q * 32 + lane, p, emit);
+         }
+         if (t1 >= ntiles) break;
+         t = t1;
+         t1 = t2;
+         t2 = t2 < ntiles && t2 + nw < ntiles ? t2 + nw : ntiles;
+         stage ^= 1;
       }
-      if (next >= ntiles) break;
-      t = next;
-      stage ^= 1;
    }
 }
 
@@ -344,8 +350,12 @@ lbm_status lbm_sparse_create(const lbm_config* cfg, int64_t nfluid, const int32_
       delete h;
       return LBM_ERR_OUT_OF_MEMORY;
    }
-   if (e == cudaSuccess) e = cudaMalloc(&h->adj, bytes);
+   // the adjacency, then the tile counter of the persistent kernel (16 bytes, zero)
+   const size_t sched_off = (bytes + 15) / 16 * 16;
+   if (e == cudaSuccess) e = cudaMalloc(&h->adj, sched_off + 16);
    if (e == cudaSuccess) e = cudaMemcpy(h->adj, adjacency, bytes, cudaMemcpyHostToDevice);
+   if (e == cudaSuccess) e = cudaMemset(reinterpret_cast<char*>(h->adj) + sched_off, 0, 16);
+   if (e == cudaSuccess) h->params.sched = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(h->adj) + sched_off);
    if (e != cudaSuccess) {
       cudaGetLastError();
       if (h->adj) cudaFree(h->adj);

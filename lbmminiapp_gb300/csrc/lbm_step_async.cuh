@@ -155,40 +155,52 @@ __global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<
    const int warp = threadIdx.x >> 5;
    constexpr int kWarps = async_warps<Q, KIND>();
    const uint32_t nw = gridDim.x * kWarps;
-   uint32_t t = blockIdx.x * kWarps + warp;
-   if (t >= ag.ntiles) return;
+   const uint32_t ntiles = ag.ntiles;
    wait_prior_grid();
    unsigned long long* mine = async_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 8;
-   TileLane cur;
-   tile_lane<LINKS, RAGGED>(p, ag, t, lane, LINKS ? tile_link(p, ag, t, lane) : 0u, cur);
-   uint32_t lk_ahead = (LINKS && t + nw < ag.ntiles) ? tile_link(p, ag, t + nw, lane) : 0u;
-   async_issue<Q, KIND, LINKS, RAGGED>(pp, cur, lane, sbase);
-   cp_async_commit();
-   int stage = 0;
-   for (;;) {
-      const uint32_t next = t + nw;
-      TileLane nxt = cur;
-      if (next < ag.ntiles) {
-         tile_lane<LINKS, RAGGED>(p, ag, next, lane, lk_ahead, nxt);
-         if (LINKS && next + nw < ag.ntiles) lk_ahead = tile_link(p, ag, next + nw, lane);
-         async_issue<Q, KIND, LINKS, RAGGED>(pp, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
-      }
+   // tiles in a fixed round-robin, or with link words (cells whose cost
+   // differs) three per warp in a fixed order and then the launch's tile
+   // feed; t is collided while t1's populations are in flight and t2's link
+   // words are loaded
+   TileFeed feed{0u, false};
+   if (LINKS) feed = feed_start(p.sched, 3u * nw, ntiles, lane);
+   uint32_t t = blockIdx.x * kWarps + warp;
+   if (t < ntiles) {
+      uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
+      uint32_t t2 = t + 2u * nw < ntiles ? t + 2u * nw : ntiles;
+      TileLane cur;
+      tile_lane<LINKS, RAGGED>(p, ag, t, lane, LINKS ? tile_link(p, ag, t, lane) : 0u, cur);
+      uint32_t lk_ahead = (LINKS && t1 < ntiles) ? tile_link(p, ag, t1, lane) : 0u;
+      async_issue<Q, KIND, LINKS, RAGGED>(pp, cur, lane, sbase);
       cp_async_commit();
-      cp_async_wait_prev();
-      if (!(LINKS || RAGGED) || cur.active) {
-         // each output is stored as the collision makes it, and the update
-         // re-reads its inputs from shared memory: neither the Q input nor the
-         // Q output patterns stay in registers
-         StoreEmit<Q, KIND, LINKS> emit{pp, cur.ci, cur.lk};
-         collide_f64x_shared_emit<Q>(mine + stage * Q * 32 + lane, p, emit);
+      int stage = 0;
+      for (;;) {
+         TileLane nxt = cur;
+         if (t1 < ntiles) {
+            tile_lane<LINKS, RAGGED>(p, ag, t1, lane, lk_ahead, nxt);
+            if (LINKS && t2 < ntiles) lk_ahead = tile_link(p, ag, t2, lane);
+            async_issue<Q, KIND, LINKS, RAGGED>(pp, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
+         }
+         cp_async_commit();
+         cp_async_wait_prev();
+         if (!(LINKS || RAGGED) || cur.active) {
+            // each output is stored as the collision makes it, and the update
+            // re-reads its inputs from shared memory: neither the Q input nor the
+            // Q output patterns stay in registers
+            StoreEmit<Q, KIND, LINKS> emit{pp, cur.ci, cur.lk};
+            collide_f64x_shared_emit<Q>(mine + stage * Q * 32 + lane, p, emit);
+         }
+         if (t1 >= ntiles) break;
+         t = t1;
+         t1 = t2;
+         if (t2 < ntiles) t2 = LINKS ? feed_next(feed, p.sched, 3u * nw, ntiles, lane) : (t2 + nw < ntiles ? t2 + nw : ntiles);
+         cur = nxt;
+         stage ^= 1;
       }
-      if (next >= ag.ntiles) break;
-      t = next;
-      cur = nxt;
-      stage ^= 1;
    }
+   if (LINKS) feed_done(p.sched);
 }
 
 inline AsyncGeom async_geom(int nx, int ny, int nz)

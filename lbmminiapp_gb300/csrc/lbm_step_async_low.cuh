@@ -90,49 +90,60 @@ __global__ void __launch_bounds__(kAsyncLowWarps * 32) step_async_low_kernel(
    const int lane = threadIdx.x & 31;
    const int warp = threadIdx.x >> 5;
    const uint32_t nw = gridDim.x * kAsyncLowWarps;
-   uint32_t t = blockIdx.x * kAsyncLowWarps + warp;
-   if (t >= ag.ntiles) return;
+   const uint32_t ntiles = ag.ntiles;
    wait_prior_grid();
    uint32_t* mine = async_low_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 4;
-   TileLane cur;
-   tile_lane<LINKS, RAGGED>(p, ag, t, lane, LINKS ? tile_link(p, ag, t, lane) : 0u, cur);
-   uint32_t lk_ahead = (LINKS && t + nw < ag.ntiles) ? tile_link(p, ag, t + nw, lane) : 0u;
-   uint32_t halves = async_issue_low<Q, ST, KIND, LINKS, RAGGED>(pp, cur, lane, sbase);
-   cp_async_commit();
-   int stage = 0;
-   for (;;) {
-      const uint32_t next = t + nw;
-      TileLane nxt = cur;
-      uint32_t halves_next = 0u;
-      if (next < ag.ntiles) {
-         tile_lane<LINKS, RAGGED>(p, ag, next, lane, lk_ahead, nxt);
-         if (LINKS && next + nw < ag.ntiles) lk_ahead = tile_link(p, ag, next + nw, lane);
-         halves_next = async_issue_low<Q, ST, KIND, LINKS, RAGGED>(pp, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
-      }
+   // tiles in a fixed round-robin, or with link words (cells whose cost
+   // differs) three per warp in a fixed order and then the launch's tile feed
+   TileFeed feed{0u, false};
+   if (LINKS) feed = feed_start(p.sched, 3u * nw, ntiles, lane);
+   uint32_t t = blockIdx.x * kAsyncLowWarps + warp;
+   if (t < ntiles) {
+      uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
+      uint32_t t2 = t + 2u * nw < ntiles ? t + 2u * nw : ntiles;
+      TileLane cur;
+      tile_lane<LINKS, RAGGED>(p, ag, t, lane, LINKS ? tile_link(p, ag, t, lane) : 0u, cur);
+      uint32_t lk_ahead = (LINKS && t1 < ntiles) ? tile_link(p, ag, t1, lane) : 0u;
+      uint32_t halves = async_issue_low<Q, ST, KIND, LINKS, RAGGED>(pp, cur, lane, sbase);
       cp_async_commit();
-      cp_async_wait_prev();
-      if (!(LINKS || RAGGED) || cur.active) {
-         float g[Q], o[Q];
-         const uint32_t* sm = mine + stage * Q * 32;
-#pragma unroll
-         for (int s = 0; s < Q; s++) g[s] = word_value<ST>(sm[s * 32 + lane], (halves >> s) & 1u);
-         if (p.forced) collide_f32<Q, ST, true>(g, o, p.Ff[0], p.Ff[1], p.Ff[2], 0.0f, p);
-         else collide_f32<Q, ST, false>(g, o, 0.0f, 0.0f, 0.0f, 0.0f, p);
-         const uint32_t c = (uint32_t)cur.ci.c;
-#pragma unroll
-         for (int s = 0; s < Q; s++) {
-            const Access a = write_access<Q, KIND, LINKS>(cur.ci, cur.lk, s);
-            store_raw(pp.dst + ((uint32_t)a.slot * pp.plane + c + (uint32_t)a.off), o[s]);
+      int stage = 0;
+      for (;;) {
+         TileLane nxt = cur;
+         uint32_t halves_next = 0u;
+         if (t1 < ntiles) {
+            tile_lane<LINKS, RAGGED>(p, ag, t1, lane, lk_ahead, nxt);
+            if (LINKS && t2 < ntiles) lk_ahead = tile_link(p, ag, t2, lane);
+            halves_next =
+               async_issue_low<Q, ST, KIND, LINKS, RAGGED>(pp, nxt, lane, sbase + (stage ^ 1) * kStageBytes);
          }
+         cp_async_commit();
+         cp_async_wait_prev();
+         if (!(LINKS || RAGGED) || cur.active) {
+            float g[Q], o[Q];
+            const uint32_t* sm = mine + stage * Q * 32;
+#pragma unroll
+            for (int s = 0; s < Q; s++) g[s] = word_value<ST>(sm[s * 32 + lane], (halves >> s) & 1u);
+            if (p.forced) collide_f32<Q, ST, true>(g, o, p.Ff[0], p.Ff[1], p.Ff[2], 0.0f, p);
+            else collide_f32<Q, ST, false>(g, o, 0.0f, 0.0f, 0.0f, 0.0f, p);
+            const uint32_t c = (uint32_t)cur.ci.c;
+#pragma unroll
+            for (int s = 0; s < Q; s++) {
+               const Access a = write_access<Q, KIND, LINKS>(cur.ci, cur.lk, s);
+               store_raw(pp.dst + ((uint32_t)a.slot * pp.plane + c + (uint32_t)a.off), o[s]);
+            }
+         }
+         if (t1 >= ntiles) break;
+         t = t1;
+         t1 = t2;
+         if (t2 < ntiles) t2 = LINKS ? feed_next(feed, p.sched, 3u * nw, ntiles, lane) : (t2 + nw < ntiles ? t2 + nw : ntiles);
+         cur = nxt;
+         halves = halves_next;
+         stage ^= 1;
       }
-      if (next >= ag.ntiles) break;
-      t = next;
-      cur = nxt;
-      halves = halves_next;
-      stage ^= 1;
    }
+   if (LINKS) feed_done(p.sched);
 }
 
 template <int Q, int ST, int KIND, bool LINKS, bool RAGGED>
