@@ -581,9 +581,9 @@ lbm_status lbm_create(const lbm_config* cfg, lbm_handle** out)
       st = dev_alloc(h, (void**)&h->partials, plane_bytes > loss_bytes ? plane_bytes : loss_bytes);
    }
    if (st == LBM_OK) st = dev_alloc(h, (void**)&h->reduce_out, sizeof(double) * 4);
-   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->sched, 16);
+   if (st == LBM_OK) st = dev_alloc(h, (void**)&h->sched, 4 * kFeedWords);
    if (st == LBM_OK) {
-      const cudaError_t e = cudaMemset(h->sched, 0, 16);
+      const cudaError_t e = cudaMemset(h->sched, 0, 4 * kFeedWords);
       if (e != cudaSuccess) st = cuda_fail(h, e, "cudaMemset");
    }
    if (st == LBM_OK) st = lbm_set_solid(h, nullptr);

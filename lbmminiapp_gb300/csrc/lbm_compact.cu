@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_even_kernel(con
       }
    };
    // tiles: two per warp in a fixed order, then the launch's tile feed
-   TileFeed feed = feed_start(p.sched, 2u * nw, ntiles, lane);
+   TileFeed feed = feed_start(p.sched, 2u * nw, ntiles, blockIdx.x * kCompactWarps + warp, nw, 1u, lane);
    uint32_t t = blockIdx.x * kCompactWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(cons
    const uint32_t meta_s = (uint32_t)__cvta_generic_to_shared(meta);
    constexpr uint32_t kStageBytes = Q * 32 * 4;
    constexpr uint32_t kSlotBytes = kMetaWords * 4;
-   TileFeed feed = feed_start(p.sched, 3u * nw, ntiles, lane);
+   TileFeed feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kCompactWarps + warp, nw, kFeedGroups, lane);
    uint32_t t = blockIdx.x * kCompactWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;

@@ -20,26 +20,40 @@ __device__ __forceinline__ void wait_prior_grid() { asm volatile("griddepcontrol
 
 // Tile order of the persistent step kernels whose tiles differ in cost (link
 // words and bounce-back, partial tiles).  Warp w of nw takes its first K tiles
-// in a fixed order (w, w + nw, ..., w + (K - 1) nw) and the rest, first = K nw,
-// first + 1, ..., from a counter (sched[0], zero at launch) as it asks for
+// in a fixed order (w, w + nw, ..., w + (K - 1) nw) and the rest as it asks for
 // them, so warps on faster SMs take more tiles and the SMs finish together: a
 // fixed round-robin to the end left the last SMs working alone for 5 to 10 %
-// of such a step.  (Where every tile costs the same, the fixed order is kept:
-// the counter's atomics cost more than they save.)  Lane 0 asks one tile
-// ahead, so the atomic's latency hides behind a tile of work.  A warp keeps
-// calling feed_next() until it returns ntiles; every thread of the block then
-// calls feed_done(), and the last block to get there sets both counter words
-// back to zero for the next launch.  All calls are warp-uniform and come after
-// wait_prior_grid().
+// of such a step, and let the warps drift apart far enough to lose the L2
+// reuse between neighbouring rows.  (Where every tile costs the same, the
+// fixed order is kept: the atomics cost more than they save.)  The tiles
+// past first = K nw are dealt to ng = min(groups, nw) interleaved groups (tile
+// first + j ng + g to group g), each with its own counter, which warp w draws
+// from for g = w mod ng.  A kernel that takes many small tiles (the compact
+// odd step, about 0.7 G tiles/s) made a single counter's address the
+// bottleneck; for the others one counter keeps neighbouring tiles together
+// and runs faster.  Lane 0 asks one tile ahead, so the atomic's
+// latency hides behind a tile of work.  A warp keeps calling feed_next() until
+// it returns ntiles; every thread of the block then calls feed_done(), and the
+// last block to get there sets the counters back to zero for the next launch.
+// All calls are warp-uniform and come after wait_prior_grid().
+constexpr uint32_t kFeedGroups = 8;
+constexpr uint32_t kFeedStride = 32;                                   // words: one 128-byte line per counter
+constexpr uint32_t kFeedWords = (kFeedGroups + 1) * kFeedStride;       // the counters and the finished-block count
+
 struct TileFeed {
-   uint32_t pend;   // lane 0: the counter value of the next dynamic tile
+   uint32_t pend;   // lane 0: the group counter's value for the next dynamic tile
+   uint32_t g;      // the warp's group
+   uint32_t ng;     // groups: kFeedGroups, fewer when the grid has fewer warps
    bool more;
 };
 
-__device__ __forceinline__ TileFeed feed_start(uint32_t* sched, uint32_t first, uint32_t ntiles, int lane)
+// groups: 1 to kFeedGroups counters (more for kernels that take many small tiles)
+__device__ __forceinline__ TileFeed feed_start(uint32_t* sched, uint32_t first, uint32_t ntiles, uint32_t w,
+                                               uint32_t nw, uint32_t groups, int lane)
 {
-   TileFeed f{0u, first < ntiles};
-   if (f.more && lane == 0) f.pend = atomicAdd(sched, 1u);
+   const uint32_t ng = nw < groups ? nw : groups;
+   TileFeed f{0u, w % ng, ng, first + w % ng < ntiles};
+   if (f.more && lane == 0) f.pend = atomicAdd(sched + f.g * kFeedStride, 1u);
    return f;
 }
 
@@ -49,12 +63,13 @@ __device__ __forceinline__ uint32_t feed_next(TileFeed& f, uint32_t* sched, uint
 {
    if (!f.more) return ntiles;
    const uint32_t v = __shfl_sync(0xFFFFFFFFu, f.pend, 0);
-   if (v >= ntiles - first) {
+   // first + v ng + g < ntiles, without overflow
+   if (v >= (ntiles - first - f.g + f.ng - 1u) / f.ng) {
       f.more = false;
       return ntiles;
    }
-   if (lane == 0) f.pend = atomicAdd(sched, 1u);
-   return first + v;
+   if (lane == 0) f.pend = atomicAdd(sched + f.g * kFeedStride, 1u);
+   return first + v * f.ng + f.g;
 }
 
 __device__ __forceinline__ void feed_done(uint32_t* sched)
@@ -62,9 +77,8 @@ __device__ __forceinline__ void feed_done(uint32_t* sched)
    __syncthreads();
    if (threadIdx.x != 0) return;
    __threadfence();
-   if (atomicAdd(sched + 1, 1u) == gridDim.x - 1u) {
-      atomicExch(sched, 0u);
-      atomicExch(sched + 1, 0u);
+   if (atomicAdd(sched + kFeedGroups * kFeedStride, 1u) == gridDim.x - 1u) {
+      for (uint32_t g = 0; g <= kFeedGroups; g++) atomicExch(sched + g * kFeedStride, 0u);
    }
 }
 

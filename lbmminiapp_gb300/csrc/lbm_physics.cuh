@@ -56,7 +56,7 @@ struct KParams {
    float x_om2w[4][2];            // (1 - omega/2) w per weight class
    float x_om2w36[2];             // (1 - omega/2) / 36
    int forced;                    // uniform force nonzero
-   uint32_t* sched;               // [2] tile counter of the persistent kernels, zero between launches
+   uint32_t* sched;               // [kFeedWords] tile counters of the persistent kernels, zero between launches
 };
 
 // Link word: bit s set when the neighbour at x + c_s is solid or outside a

@@ -350,11 +350,11 @@ lbm_status lbm_sparse_create(const lbm_config* cfg, int64_t nfluid, const int32_
       delete h;
       return LBM_ERR_OUT_OF_MEMORY;
    }
-   // the adjacency, then the tile counter of the persistent kernel (16 bytes, zero)
-   const size_t sched_off = (bytes + 15) / 16 * 16;
-   if (e == cudaSuccess) e = cudaMalloc(&h->adj, sched_off + 16);
+   // the adjacency, then the tile counters of the persistent kernels (zero)
+   const size_t sched_off = (bytes + 127) / 128 * 128;
+   if (e == cudaSuccess) e = cudaMalloc(&h->adj, sched_off + 4 * kFeedWords);
    if (e == cudaSuccess) e = cudaMemcpy(h->adj, adjacency, bytes, cudaMemcpyHostToDevice);
-   if (e == cudaSuccess) e = cudaMemset(reinterpret_cast<char*>(h->adj) + sched_off, 0, 16);
+   if (e == cudaSuccess) e = cudaMemset(reinterpret_cast<char*>(h->adj) + sched_off, 0, 4 * kFeedWords);
    if (e == cudaSuccess) h->params.sched = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(h->adj) + sched_off);
    if (e != cudaSuccess) {
       cudaGetLastError();

@@ -164,8 +164,8 @@ __global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<
    // differs) three per warp in a fixed order and then the launch's tile
    // feed; t is collided while t1's populations are in flight and t2's link
    // words are loaded
-   TileFeed feed{0u, false};
-   if (LINKS) feed = feed_start(p.sched, 3u * nw, ntiles, lane);
+   TileFeed feed{0u, 0u, 1u, false};
+   if (LINKS) feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kWarps + warp, nw, 1u, lane);
    uint32_t t = blockIdx.x * kWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;

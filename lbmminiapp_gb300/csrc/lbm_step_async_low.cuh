@@ -97,8 +97,8 @@ __global__ void __launch_bounds__(kAsyncLowWarps * 32) step_async_low_kernel(
    constexpr uint32_t kStageBytes = Q * 32 * 4;
    // tiles in a fixed round-robin, or with link words (cells whose cost
    // differs) three per warp in a fixed order and then the launch's tile feed
-   TileFeed feed{0u, false};
-   if (LINKS) feed = feed_start(p.sched, 3u * nw, ntiles, lane);
+   TileFeed feed{0u, 0u, 1u, false};
+   if (LINKS) feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kAsyncLowWarps + warp, nw, 1u, lane);
    uint32_t t = blockIdx.x * kAsyncLowWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
