@@ -147,7 +147,9 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_even_kernel(con
       }
    };
    // tiles: two per warp in a fixed order, then the launch's tile feed
-   TileFeed feed = feed_start(p.sched, 2u * nw, ntiles, blockIdx.x * kCompactWarps + warp, nw, 1u, lane);
+   const bool fed = feed_on(ntiles, nw);
+   TileFeed feed{0u, 0u, 1u, false};
+   if (fed) feed = feed_start(p.sched, 2u * nw, ntiles, blockIdx.x * kCompactWarps + warp, nw, 1u, lane);
    uint32_t t = blockIdx.x * kCompactWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
@@ -171,11 +173,11 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_even_kernel(con
          }
          if (t1 >= ntiles) break;
          t = t1;
-         t1 = feed_next(feed, p.sched, 2u * nw, ntiles, lane);
+         t1 = feed_after(feed, fed, t1, p.sched, 2u * nw, ntiles, nw, lane);
          stage ^= 1;
       }
    }
-   feed_done(p.sched);
+   if (fed) feed_done(p.sched);
 }
 
 // ------------------------------------------------------------------ odd
@@ -280,9 +282,9 @@ __device__ __forceinline__ uint32_t odd_pop_issue(const T* buf, const CompactGeo
    return halves;
 }
 
-// Tiles come from the launch's tile feed (lbm_launch.cuh): three per warp in
-// a fixed order, the rest as the warps ask for them (tiles differ in cost:
-// bounce-back, partial tiles).
+// Tiles: three per warp in a fixed order, the rest from the launch's tile
+// feed (lbm_launch.cuh) with 8 counters (tiles differ in cost: bounce-back,
+// partial tiles; and they are small, so one counter would be the bottleneck).
 template <int Q, int ST, bool FORCE>
 __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(const KParams p, const CompactGeom g,
                                                                             typename Store<ST>::T* buf)
@@ -299,7 +301,9 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(cons
    const uint32_t meta_s = (uint32_t)__cvta_generic_to_shared(meta);
    constexpr uint32_t kStageBytes = Q * 32 * 4;
    constexpr uint32_t kSlotBytes = kMetaWords * 4;
-   TileFeed feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kCompactWarps + warp, nw, kFeedGroups, lane);
+   const bool fed = feed_on(ntiles, nw);
+   TileFeed feed{0u, 0u, 1u, false};
+   if (fed) feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kCompactWarps + warp, nw, kFeedGroups, lane);
    uint32_t t = blockIdx.x * kCompactWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
@@ -319,7 +323,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(cons
       uint32_t slot = 0, stage = 0;
       for (;;) {
          const uint32_t slot1 = slot == 2 ? 0 : slot + 1, slot2 = slot1 == 2 ? 0 : slot1 + 1;
-         const uint32_t t3 = t2 < ntiles ? feed_next(feed, p.sched, 3u * nw, ntiles, lane) : ntiles;
+         const uint32_t t3 = feed_after(feed, fed, t2, p.sched, 3u * nw, ntiles, nw, lane);
          // this tile's populations and the next tile's metadata have landed
          cp_async_wait_all();
          __syncwarp();
@@ -353,7 +357,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2) compact_odd_kernel(cons
          stage ^= 1u;
       }
    }
-   feed_done(p.sched);
+   if (fed) feed_done(p.sched);
 }
 
 // Persistent grid: as many blocks as fit on the device at once, queried once

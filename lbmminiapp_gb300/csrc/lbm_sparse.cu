@@ -185,8 +185,14 @@ __global__ void __launch_bounds__(kSparseAsyncWarps * 32, kSparseAsyncBlocks) sp
          cp_async8(sb + (uint32_t)(s * 32 + lane) * 8u, s64 + r);
       }
    };
-   // tiles in a fixed round-robin: t is collided while t1's populations are
-   // in flight and t2's read locations are loaded
+   // tiles: three per warp in a fixed order, then the launch's tile feed (8
+   // counters for the D3Q19 tiles, which it hands out fastest); t is collided
+   // while t1's populations are in flight and t2's read locations are loaded
+   const bool fed = feed_on(ntiles, nw);
+   TileFeed feed{0u, 0u, 1u, false};
+   if (fed)
+      feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kSparseAsyncWarps + warp, nw,
+                        Q == 19 ? kFeedGroups : 1u, lane);
    uint32_t t = blockIdx.x * kSparseAsyncWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
@@ -220,10 +226,11 @@ __global__ void __launch_bounds__(kSparseAsyncWarps * 32, kSparseAsyncBlocks) sp
          if (t1 >= ntiles) break;
          t = t1;
          t1 = t2;
-         t2 = t2 < ntiles && t2 + nw < ntiles ? t2 + nw : ntiles;
+         t2 = feed_after(feed, fed, t2, p.sched, 3u * nw, ntiles, nw, lane);
          stage ^= 1;
       }
    }
+   if (fed) feed_done(p.sched);
 }
 
 template <int Q, int KIND>

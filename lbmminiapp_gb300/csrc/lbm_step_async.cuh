@@ -160,12 +160,12 @@ __global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<
    unsigned long long* mine = async_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 8;
-   // tiles in a fixed round-robin, or with link words (cells whose cost
-   // differs) three per warp in a fixed order and then the launch's tile
-   // feed; t is collided while t1's populations are in flight and t2's link
-   // words are loaded
+   // tiles: three per warp in a fixed order, then the launch's tile feed (8
+   // counters for the D3Q19 tiles, which it hands out fastest); t is collided
+   // while t1's populations are in flight and t2's link words are loaded
+   const bool fed = feed_on(ntiles, nw);
    TileFeed feed{0u, 0u, 1u, false};
-   if (LINKS) feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kWarps + warp, nw, 1u, lane);
+   if (fed) feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kWarps + warp, nw, Q == 19 ? kFeedGroups : 1u, lane);
    uint32_t t = blockIdx.x * kWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
@@ -195,12 +195,12 @@ __global__ void __launch_bounds__(async_warps<Q, KIND>() * 32, async_min_blocks<
          if (t1 >= ntiles) break;
          t = t1;
          t1 = t2;
-         if (t2 < ntiles) t2 = LINKS ? feed_next(feed, p.sched, 3u * nw, ntiles, lane) : (t2 + nw < ntiles ? t2 + nw : ntiles);
+         t2 = feed_after(feed, fed, t2, p.sched, 3u * nw, ntiles, nw, lane);
          cur = nxt;
          stage ^= 1;
       }
    }
-   if (LINKS) feed_done(p.sched);
+   if (fed) feed_done(p.sched);
 }
 
 inline AsyncGeom async_geom(int nx, int ny, int nz)

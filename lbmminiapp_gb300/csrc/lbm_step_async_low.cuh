@@ -95,10 +95,10 @@ __global__ void __launch_bounds__(kAsyncLowWarps * 32) step_async_low_kernel(
    uint32_t* mine = async_low_smem + (size_t)warp * kAsyncStages * Q * 32;
    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(mine);
    constexpr uint32_t kStageBytes = Q * 32 * 4;
-   // tiles in a fixed round-robin, or with link words (cells whose cost
-   // differs) three per warp in a fixed order and then the launch's tile feed
+   // tiles: three per warp in a fixed order, then the launch's tile feed
+   const bool fed = feed_on(ntiles, nw);
    TileFeed feed{0u, 0u, 1u, false};
-   if (LINKS) feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kAsyncLowWarps + warp, nw, 1u, lane);
+   if (fed) feed = feed_start(p.sched, 3u * nw, ntiles, blockIdx.x * kAsyncLowWarps + warp, nw, 1u, lane);
    uint32_t t = blockIdx.x * kAsyncLowWarps + warp;
    if (t < ntiles) {
       uint32_t t1 = t + nw < ntiles ? t + nw : ntiles;
@@ -137,13 +137,13 @@ __global__ void __launch_bounds__(kAsyncLowWarps * 32) step_async_low_kernel(
          if (t1 >= ntiles) break;
          t = t1;
          t1 = t2;
-         if (t2 < ntiles) t2 = LINKS ? feed_next(feed, p.sched, 3u * nw, ntiles, lane) : (t2 + nw < ntiles ? t2 + nw : ntiles);
+         t2 = feed_after(feed, fed, t2, p.sched, 3u * nw, ntiles, nw, lane);
          cur = nxt;
          halves = halves_next;
          stage ^= 1;
       }
    }
-   if (LINKS) feed_done(p.sched);
+   if (fed) feed_done(p.sched);
 }
 
 template <int Q, int ST, int KIND, bool LINKS, bool RAGGED>
