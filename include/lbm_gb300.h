@@ -111,7 +111,10 @@ void lbm_destroy(lbm_handle* h);
 const char* lbm_last_error(const lbm_handle* h); /* never NULL */
 const char* lbm_status_string(lbm_status s);
 lbm_status lbm_get_info(const lbm_handle* h, lbm_info* info);
-/* cudaStream_t passed as void*; NULL = the legacy default stream. */
+/* cudaStream_t passed as void*; NULL = the legacy default stream.  A handle's
+ * step kernels share its tile counters (zero between launches), so its steps
+ * run in one stream order: after switching streams, order the new stream after
+ * the old one's last step (an event) before the next step. */
 lbm_status lbm_set_stream(lbm_handle* h, void* stream);
 lbm_status lbm_synchronize(lbm_handle* h);
 
@@ -233,6 +236,8 @@ lbm_status lbm_sparse_create(const lbm_config* cfg, int64_t nfluid, const int32_
                              lbm_sparse_handle** out);
 void lbm_sparse_destroy(lbm_sparse_handle* h);
 const char* lbm_sparse_last_error(const lbm_sparse_handle* h); /* never NULL */
+/* As lbm_set_stream: the handle's steps share its tile counters and run in one
+ * stream order. */
 lbm_status lbm_sparse_set_stream(lbm_sparse_handle* h, void* stream);
 /* KernelAA::timestepEvenForce(Pdf* dstrb, int startIdx, int countIdx)
  * (src/kernels/KernelAA.hh:28) on a compact device buffer of Q*nfluid doubles */

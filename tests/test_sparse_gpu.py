@@ -124,6 +124,30 @@ def test_matches_dense_layout_on_larger_cylinder(gpu, Q, pattern, arithmetic):
     assert np.array_equal(out, dense)
 
 
+@pytest.mark.parametrize("Q,pattern", [(19, "aa"), (19, "ab_pull"), (27, "aa"), (27, "ab_push")])
+def test_matches_dense_layout_with_tile_feed(gpu, Q, pattern):
+    """The same comparison in F64X on a size-4 cylinder (about 1.15 million
+    fluid points): at least 16 tiles per warp, so both layouts' persistent
+    kernels take their tiles from the tile feed after the fixed first round,
+    over 9 steps (each launch re-arms the feed's counters for the next)."""
+    import lbmminiapp_gb300 as lbm
+    dims, solid = cylinder(4.0)
+    nx, ny, nz = dims
+    cells, adj = sparse.build_adjacency(solid, (1, 0, 0), pattern, Q)
+    assert adj.shape[1] >= 16 * 32 * 152 * 12   # tiles per warp of the 12-warp-per-SM kernel
+    omega, gx, steps = 1.0 / 0.6, 1e-5, 9
+    with lbm.Simulation(nx, ny, nz, lattice=Q, pattern=pattern, omega=omega, force=(gx, 0, 0),
+                        periodic=(1, 0, 0), arithmetic="f64x") as sim:
+        sim.set_solid(solid)
+        sim.init_equilibrium(None, None)
+        sim.step(steps)
+        dense = sim.get_populations("raw").reshape(Q, -1)[:, cells]
+    g = dict(Q=Q, prop_pattern=1 if pattern == "aa" else 0, pull=int(pattern == "ab_pull"), omega=omega,
+             gx=gx, steps=steps, adjacency=adj)
+    out = run_case(g, "f64x")
+    assert np.array_equal(out, dense)
+
+
 def test_errors_are_reported(gpu):
     g = load_golden("sparse_q19_aa_cylinder")
     n = g["adjacency"].shape[1]
