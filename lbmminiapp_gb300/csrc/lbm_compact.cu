@@ -3,24 +3,27 @@
 // between the compact and the dense layouts.
 //
 // Both steps use the pipelined scheme of the dense kernels
-// (lbm_step_async_low.cuh): persistent warps, one fluid cell per lane, and the
-// populations of the next tile in flight as 4-byte cp.async copies (the
-// aligned word holding each element) into a two-stage shared buffer per warp
+// (lbm_step_async_low.cuh): persistent warps, and the populations of the next
+// tile in flight as cp.async copies into a two-stage shared buffer per warp
 // while the current tile collides.  No lane holds a solid cell, and every
-// sector moved holds fluid populations only.
+// sector moved holds fluid populations only.  Tiles come from the tile feed
+// (lbm_launch.cuh): a fixed first round, then counters.
 //
-//   even step (KernelAA_SOA_Base.cpp:173-254): tiles of 32 consecutive fluid
-//     indices; read own slot opp(s), write own slot s: contiguous accesses.
-//   odd step (KernelAA_SOA_Base.cpp:257-342): tiles of up to 32 fluid cells of
-//     one row, so the 9 neighbour rows are the same for the whole warp; read
-//     slot s at x - c_s (own slot opp(s) when that neighbour is blocked),
-//     write slot opp(s) at x + c_s (own slot s when blocked).
+//   even step (KernelAA_SOA_Base.cpp:173-254): tiles of 64 consecutive fluid
+//     indices, two cells per lane; read own slot opp(s), write own slot s, one
+//     aligned word per slot for both cells: contiguous accesses.
+//   odd step (KernelAA_SOA_Base.cpp:257-342): row tiles of up to 32 fluid
+//     cells, one per lane, so the 9 neighbour rows are the same for the whole
+//     warp; read slot s at x - c_s (own slot opp(s) when that neighbour is
+//     blocked), write slot opp(s) at x + c_s (own slot s when blocked).  Each
+//     lane copies the 4-byte word holding each of its elements; the tile's
+//     metadata is copied two tiles ahead.
 //
-// AA stays race-free under the prefetch for the dense layout's reason: a
-// cell's reads and writes touch the same set of elements, so a prefetch of
-// another tile never reads an element this tile writes.  A copied word may
-// hold a second element written by another cell; only the lane's own half is
-// used.
+// AA stays race-free under the prefetch and in any tile order for the dense
+// layout's reason: a cell's reads and writes touch the same set of elements,
+// so a prefetch of another tile never reads an element this tile writes.  A
+// copied word may hold a second element written by another cell; only the
+// lane's own half is used.
 #include <atomic>
 
 #include "lbm_compact.cuh"
