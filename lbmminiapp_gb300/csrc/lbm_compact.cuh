@@ -5,7 +5,7 @@
 //
 // Streaming needs no per-direction adjacency list.  The odd step works on
 // row tiles: up to 32 consecutive fluid cells of one row r = y + ny z whose x
-// lie within 256 of the tile's first x (xa).  Per tile, for each of the 9 rows
+// lie at most 255 past the tile's first x (xa).  Per tile, for each of the 9 rows
 // r' = r + (dy, dz) (periodic wrap of y and z), b[k] is the compact index of
 // the first fluid cell of r' at or after xa and n[k] the fluid count of r';
 // per cell, u[k] counts the fluid cells of r' in [xa, x).  The fluid cell at
