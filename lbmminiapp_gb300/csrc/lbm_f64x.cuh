@@ -483,9 +483,18 @@ struct KeepInputs {
 // FORCE is the forcing form of force_mode() (0 none, 1 added after the
 // equilibrium, 2 folded into it); Again supplies the inputs' float pairs for
 // the (1 - omega) f term (KeepInputs, or a second read from shared memory).
-template <int Q, int FORCE, class Emit, class Again>
+//
+// ROLLED (D3Q27): the 13 opposite pairs run in three loops over the pair
+// classes (axes, planar and body diagonals) instead of unrolled, with the same
+// operations in the same order, so the same bits.  The unrolled D3Q27 path is
+// about 2,700 instructions per cell, more than the instruction cache holds;
+// rolled, a third of it.  The direction and its velocity are then run-time
+// values: outputs go to emit.put(s, opp(s), c_s, pattern), and Kf points at
+// the per-direction forcing constants (float pairs, direction-indexed).
+template <int Q, int FORCE, class Emit, class Again, bool ROLLED = false>
 __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (&bits)[Q], const x64::Consts& k,
-                                                               int compat, Emit& emit, const Again& again)
+                                                               int compat, Emit& emit, const Again& again,
+                                                               const float (*Kf)[2] = nullptr)
 {
    using namespace x64;
    constexpr int R = lat_rest(Q);
@@ -600,6 +609,91 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (
       }
       emit(R, join(out, range));
    }
+   if constexpr (ROLLED) {
+      static_assert(Q == 27, "the pair-class loops follow the D3Q27 direction order");
+      // One pair (s, o = opp(s)) with c_s = (cx, cy, cz), cu = 3 c_s.v and the
+      // class constants: the unrolled loop's body below, operation for operation.
+      auto pair = [&](int s, int o, int cx, int cy, int cz, const df cu, const df owc, const df om2wc) {
+         const df c2h = df_sqr_u(cu);
+         const df qs = fast_two_sum(base.h, 0.5f * c2h.h);
+         const df Qp = {qs.h, fadd(qs.l, fadd(base.l, 0.5f * c2h.l))};
+         df A = df_mul_u(owc, Qp);
+         df B = df_mul_u(owc, cu);
+         const df Ks = {Kf[s][0], Kf[s][1]};
+         df sym = {0.f, 0.f};
+         if (FORCE) {
+            const df gc = df_mul_u(Ks, cu);
+            const df wf = df_mul_u(om2wc, fu);
+            const df t3 = two_sum(gc.h, -wf.h);
+            sym = {t3.h, fadd(t3.l, fsub(gc.l, wf.l))};
+         }
+         if (FORCE == 2) {
+            const df as = fast_two_sum(A.h, sym.h);
+            A = {as.h, fadd(as.l, fadd(A.l, sym.l))};
+            const df bs = two_sum(B.h, Ks.h);
+            B = {bs.h, fadd(bs.l, fadd(B.l, Ks.l))};
+         }
+         {
+            const df tp = fast_two_sum(A.h, B.h);
+            const df a = df_mul_u(k.om1, input_pair(f, again, s));
+            const df t = two_sum(tp.h, a.h);
+            df out = {t.h, fadd(t.l, fadd(tp.l, fadd(fadd(A.l, B.l), a.l)))};
+            if (FORCE == 1) {
+               const df fr = two_sum(Ks.h, sym.h);
+               const df t2 = two_sum(out.h, fr.h);
+               out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fadd(Ks.l, sym.l))))};
+            }
+            emit.put(s, o, cx, cy, cz, join(out, range));
+         }
+         {
+            const df tm = fast_two_sum(A.h, -B.h);
+            const df a = df_mul_u(k.om1, input_pair(f, again, o));
+            const df t = two_sum(tm.h, a.h);
+            df out = {t.h, fadd(t.l, fadd(tm.l, fadd(fsub(A.l, B.l), a.l)))};
+            if (FORCE == 1) {
+               const df fr = two_sum(sym.h, -Ks.h);
+               const df t2 = two_sum(out.h, fr.h);
+               out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fsub(sym.l, Ks.l))))};
+            }
+            emit.put(o, s, -cx, -cy, -cz, join(out, range));
+         }
+      };
+      // axes: (0,1) (2,3) (4,5), c = e_d, cu = 3 v_d
+#pragma unroll 1
+      for (int d = 0; d < 3; d++) {
+         const df cu = d == 0 ? v3[0] : (d == 1 ? v3[1] : v3[2]);
+         pair(2 * d, 2 * d + 1, d == 0, d == 1, d == 2, cu, owr[1], k.om2w[1]);
+      }
+      // planar diagonals (6,11) (7,10) (8,13) (9,12) (14,17) (15,16):
+      // c = e_a + sign e_b, a < b, sign -1 for the odd j
+#pragma unroll 1
+      for (int j = 0; j < 6; j++) {
+         const int a = j < 4 ? 0 : 1, b = j < 2 ? 1 : 2;
+         const bool neg = (j & 1) != 0;
+         const df va = a == 0 ? v3[0] : v3[1];
+         const df vb = b == 1 ? v3[1] : v3[2];
+         const df t = neg ? df_neg(vb) : vb;
+         const df u2 = two_sum(va.h, t.h);
+         const df cu = {u2.h, fadd(u2.l, fadd(va.l, t.l))};
+         const int sgn = neg ? -1 : 1;
+         const int sd = j < 4 ? 6 + j : 10 + j;
+         const int od = j < 2 ? 11 - j : (j < 4 ? 15 - j : 31 - sd);
+         pair(sd, od, a == 0 ? 1 : 0, a == 1 ? 1 : (b == 1 ? sgn : 0), b == 2 ? sgn : 0, cu, owr[2], k.om2w[2]);
+      }
+      // body diagonals (18,25) (19,24) (20,23) (21,22): c = (1, +-1, +-1)
+#pragma unroll 1
+      for (int j = 0; j < 4; j++) {
+         const bool ny = j >= 2, nz = (j & 1) != 0;
+         const df ty = ny ? df_neg(v3[1]) : v3[1];
+         const df u2 = two_sum(v3[0].h, ty.h);
+         df cu = {u2.h, fadd(u2.l, fadd(v3[0].l, ty.l))};
+         const df tz = nz ? df_neg(v3[2]) : v3[2];
+         const df u3 = two_sum(cu.h, tz.h);
+         cu = {u3.h, fadd(u3.l, fadd(cu.l, tz.l))};
+         pair(18 + j, 25 - j, 1, ny ? -1 : 1, nz ? -1 : 1, cu, owr[3], k.om2w[3]);
+      }
+      return range.ok();
+   }
 #pragma unroll
    for (int q = 0; q < NP; q++) {
       const int s = pair_dir(Q, q), o = lat_opp(Q, s);
@@ -676,6 +770,7 @@ template <int Q>
 struct EmitToArray {
    uint64_t res[Q];
    __host__ __device__ __forceinline__ void operator()(int s, uint64_t v) { res[s] = v; }
+   __host__ __device__ __forceinline__ void put(int s, int, int, int, int, uint64_t v) { res[s] = v; }
 };
 
 
@@ -763,7 +858,9 @@ struct AgainFromShared {
 // over them (the fallback reads its inputs from shared memory): a caller's
 // emit must let a later emit of the same s win, as stores from one thread to
 // one address do.
-template <int Q, class Emit>
+// ROLLED: the D3Q27 pair-class loops (collide_f64x_fast_emit), whose outputs
+// go to emit.put.
+template <int Q, bool ROLLED = false, class Emit>
 __device__ __forceinline__ void collide_f64x_shared_emit(const unsigned long long* in, const KParams& p, Emit& emit)
 {
    uint64_t bits[Q];
@@ -771,9 +868,11 @@ __device__ __forceinline__ void collide_f64x_shared_emit(const unsigned long lon
    for (int s = 0; s < Q; s++) bits[s] = in[s * 32];
    const x64::Consts k = collide_consts<Q>(p);
    const AgainFromShared again{(uint32_t)__cvta_generic_to_shared(in)};
-   const bool fast = p.forced == 2 ? collide_f64x_fast_emit<Q, 2>(bits, k, p.compat, emit, again)
-                     : p.forced    ? collide_f64x_fast_emit<Q, 1>(bits, k, p.compat, emit, again)
-                                   : collide_f64x_fast_emit<Q, 0>(bits, k, p.compat, emit, again);
+   using A = AgainFromShared;
+   const bool fast =
+      p.forced == 2 ? collide_f64x_fast_emit<Q, 2, Emit, A, ROLLED>(bits, k, p.compat, emit, again, p.x_Kf)
+      : p.forced    ? collide_f64x_fast_emit<Q, 1, Emit, A, ROLLED>(bits, k, p.compat, emit, again, p.x_Kf)
+                    : collide_f64x_fast_emit<Q, 0, Emit, A, ROLLED>(bits, k, p.compat, emit, again, p.x_Kf);
    if (fast) return;
 #pragma unroll
    for (int s = 0; s < Q; s++) bits[s] = again.raw(s);

@@ -99,6 +99,17 @@ __device__ __forceinline__ Access write_access(const CellIndex& ci, uint32_t lk,
    return {s, nbr_off(ci, lat_c(Q, s, 0), lat_c(Q, s, 1), lat_c(Q, s, 2))};
 }
 
+// write_access for a non-rest direction s known at run time (o = opp(s),
+// velocity (cx, cy, cz)).
+template <int KIND, bool LINKS>
+__device__ __forceinline__ Access write_access_rt(const CellIndex& ci, uint32_t lk, int s, int o, int cx, int cy, int cz)
+{
+   if (KIND == K_AA_EVEN || KIND == K_AB_PULL) return {s, 0};
+   const bool blocked = LINKS && ((lk >> s) & 1u);
+   if (KIND == K_AA_ODD) return blocked ? Access{s, 0} : Access{o, nbr_off(ci, cx, cy, cz)};
+   return blocked ? Access{o, 0} : Access{s, nbr_off(ci, cx, cy, cz)};
+}
+
 template <typename T, typename IT>
 __device__ __forceinline__ T* slot_ptr(T* cell_base, IT plane_bytes, Access a)
 {

@@ -15,7 +15,7 @@ int force_mode_of(const double* F, double omega)
    return lbm::force_mode(f, omega);
 }
 
-template <int Q>
+template <int Q, bool ROLLED = false>
 int run(const double* in, double* out, int n, double omega, const double* F, int compat, int force_mode, int* fast)
 {
    using namespace lbm;
@@ -47,9 +47,26 @@ int run(const double* in, double* out, int n, double omega, const double* F, int
    for (int i = 0; i < n; i++) {
       uint64_t bits[Q];
       for (int s = 0; s < Q; s++) bits[s] = x64::double_bits(in[(size_t)i * Q + s]);
-      const bool ok = mode == 2 ? collide_f64x_fast<Q, 2>(bits, k, compat)
-                    : mode == 1 ? collide_f64x_fast<Q, 1>(bits, k, compat)
-                                : collide_f64x_fast<Q, 0>(bits, k, compat);
+      bool ok;
+      if constexpr (ROLLED) {
+         // the pair-class loops, with the forcing constants as a direction-indexed table
+         float Kf[Q][2];
+         for (int s = 0; s < Q; s++) {
+            Kf[s][0] = k.Kf[s].h;
+            Kf[s][1] = k.Kf[s].l;
+         }
+         EmitToArray<Q> em;
+         const KeepInputs keep{};
+         ok = mode == 2   ? collide_f64x_fast_emit<Q, 2, EmitToArray<Q>, KeepInputs, true>(bits, k, compat, em, keep, Kf)
+              : mode == 1 ? collide_f64x_fast_emit<Q, 1, EmitToArray<Q>, KeepInputs, true>(bits, k, compat, em, keep, Kf)
+                          : collide_f64x_fast_emit<Q, 0, EmitToArray<Q>, KeepInputs, true>(bits, k, compat, em, keep, Kf);
+         if (ok)
+            for (int s = 0; s < Q; s++) bits[s] = em.res[s];
+      } else {
+         ok = mode == 2   ? collide_f64x_fast<Q, 2>(bits, k, compat)
+              : mode == 1 ? collide_f64x_fast<Q, 1>(bits, k, compat)
+                          : collide_f64x_fast<Q, 0>(bits, k, compat);
+      }
       fast[i] = ok ? 1 : 0;
       nfast += ok;
       for (int s = 0; s < Q; s++)
@@ -67,4 +84,12 @@ extern "C" int f64x_collide_host(int Q, const double* in, double* out, int n, do
 {
    return Q == 19 ? run<19>(in, out, n, omega, F, compat, force_mode, fast)
                   : run<27>(in, out, n, omega, F, compat, force_mode, fast);
+}
+
+// The D3Q27 fast path with the pair-class loops (the rolled form the D3Q27
+// step kernels run); same arguments as f64x_collide_host.
+extern "C" int f64x_collide_host_q27_rolled(const double* in, double* out, int n, double omega, const double* F,
+                                            int compat, int force_mode, int* fast)
+{
+   return run<27, true>(in, out, n, omega, F, compat, force_mode, fast);
 }

@@ -27,6 +27,7 @@ def f64x(tmp_path_factory):
     P = ctypes.c_void_p
     lib.f64x_collide_host.argtypes = [ctypes.c_int, P, P, ctypes.c_int, ctypes.c_double, P, ctypes.c_int,
                                       ctypes.c_int, P]
+    lib.f64x_collide_host_q27_rolled.argtypes = [P, P, ctypes.c_int, ctypes.c_double, P, ctypes.c_int, ctypes.c_int, P]
     return lib
 
 
@@ -181,3 +182,23 @@ def test_wide_sweep_of_flow_cells(f64x, Q):
     ref = collide_exact(Q, f, 1.0 / 0.55, (0.0, 0.0, 0.0))
     assert fast.all()
     assert (np.abs(out - ref) / np.abs(ref)).max() < 2e-13
+
+
+@pytest.mark.parametrize("omega", [1.0 / 0.55, 1.25, 1.0 / 0.6, 0.7])
+@pytest.mark.parametrize("F,mode", [((0.0, 0.0, 0.0), -1), ((1e-6, 0.0, 0.0), 2), ((1e-5, -2e-6, 3e-6), 1),
+                                    ((1e-3, 5e-4, -2e-4), 2), ((3e-2, -1e-2, 1e-2), 1)])
+def test_q27_pair_class_loops_give_the_same_bits(f64x, omega, F, mode):
+    """The D3Q27 step kernels run the fast path with its 13 opposite pairs in
+    three loops over the pair classes; it must give the unrolled form's bits
+    and take the fast path for the same cells (including cells sent to the
+    exact path: fast velocities, far from equilibrium)."""
+    cells = np.concatenate([random_cells(27, 3000, 0.08, 0.02, seed=7), random_cells(27, 500, 0.3, 0.3, seed=8)])
+    want, want_fast = run(f64x, 27, cells, omega, F, force_mode=mode)
+    out = np.empty_like(cells)
+    fast = np.empty(cells.shape[0], np.int32)
+    Fa = np.asarray(F, dtype=np.float64)
+    f64x.f64x_collide_host_q27_rolled(cells.ctypes.data, out.ctypes.data, cells.shape[0], omega, Fa.ctypes.data, 0,
+                                      mode, fast.ctypes.data)
+    assert np.array_equal(fast.astype(bool), want_fast)
+    assert want_fast.mean() > 0.5 and not want_fast.all()
+    assert np.array_equal(out.view(np.uint64)[want_fast], want.view(np.uint64)[want_fast])
