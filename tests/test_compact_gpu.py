@@ -68,6 +68,37 @@ def test_compact_equals_dense(gpu, Q, storage, geometry, steps):
         assert np.array_equal(a[k], b[k], equal_nan=True), k
 
 
+@pytest.mark.parametrize("Q", [19, 27])
+def test_compact_long_sparse_rows_equal_dense(gpu, Q):
+    """Rows whose fluid cells lie 9 to 13 apart: 32 of them span more than 255
+    cells in x, so the row tiles split at the 255-cell span (their per-lane
+    counts are bytes); denser rows and a solid row around them; x open and
+    periodic."""
+    nx, ny, nz = 700, 4, 3
+    rng = np.random.default_rng(11)
+    solid = np.zeros((nz, ny, nx), np.uint8)
+    for z in range(nz):
+        for y in range(ny):
+            if (y + z) % 2 == 0:
+                row = np.ones(nx, np.uint8)
+                x = int(rng.integers(0, 9))
+                while x < nx:
+                    row[x] = 0
+                    x += int(rng.integers(9, 14))
+                solid[z, y] = row
+            else:
+                solid[z, y] = (rng.random(nx) < 0.3).astype(np.uint8)
+    solid[1, 2, :] = 1
+    u = workloads.taylor_green(nx, ny, nz, 0.04, noise=2e-3, seed=4)
+    u[:, solid.astype(bool)] = 0
+    f0 = core.equilibrium(Q, 1.0 + 0.01 * rng.random((nz, ny, nx)), u)
+    for per in ((1, 1, 1), (0, 1, 1)):
+        a = run((nx, ny, nz), Q, "f16", solid, f0, 5, per, compact=False)
+        b = run((nx, ny, nz), Q, "f16", solid, f0, 5, per, compact=True)
+        for k in ("raw", "logical", "rho", "u", "cons"):
+            assert np.array_equal(a[k], b[k], equal_nan=True), (per, k)
+
+
 def test_compact_without_force_equals_dense(gpu):
     dims, per = (24, 8, 6), (1, 1, 1)
     solid, f0 = case(27, dims, False, 0.3, seed=3)
