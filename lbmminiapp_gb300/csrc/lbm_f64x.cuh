@@ -486,9 +486,10 @@ struct KeepInputs {
 //
 // ROLLED (D3Q27): the 13 opposite pairs run in three loops over the pair
 // classes (axes, planar and body diagonals) instead of unrolled, with the same
-// operations in the same order, so the same bits.  The unrolled D3Q27 path is
-// about 2,700 instructions per cell, more than the instruction cache holds;
-// rolled, a third of it.  The direction and its velocity are then run-time
+// operations in the same order, so the same bits.  The unrolled D3Q27 path
+// runs about 2,700 instructions per cell, more code than the instruction cache
+// holds; rolled, the pair code exists once per class instead of once per
+// pair.  The direction and its velocity are then run-time
 // values: outputs go to emit.put(s, opp(s), c_s, pattern), and Kf points at
 // the per-direction forcing constants (float pairs, direction-indexed).
 template <int Q, int FORCE, class Emit, class Again, bool ROLLED = false>
