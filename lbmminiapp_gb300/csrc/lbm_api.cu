@@ -338,71 +338,10 @@ void free_compact(lbm_handle* h)
 // are gathered from the dense ones.
 lbm_status build_compact(lbm_handle* h, const uint8_t* solid)
 {
-   const int nx = h->cfg.nx, ny = h->cfg.ny, nz = h->cfg.nz;
-   const int64_t nrows = (int64_t)ny * nz;
-   // per row: first compact index and fluid count; per cell: fluid cells
-   // before it in its row
-   std::vector<uint32_t> dcell, rstart((size_t)nrows), rcount((size_t)nrows);
-   std::vector<uint16_t> pre((size_t)h->ncell);
-   dcell.reserve((size_t)h->nfluid);
-   for (int64_t r = 0; r < nrows; r++) {
-      rstart[(size_t)r] = (uint32_t)dcell.size();
-      uint32_t cnt = 0;
-      for (int x = 0; x < nx; x++) {
-         const int64_t c = r * nx + x;
-         pre[(size_t)c] = (uint16_t)cnt;
-         if (!solid || !solid[c]) {
-            dcell.push_back((uint32_t)c);
-            cnt++;
-         }
-      }
-      rcount[(size_t)r] = cnt;
-   }
-   // row tiles: up to 32 consecutive fluid cells of a row within 255 of the
-   // first one's x, so the per-lane counts fit a byte
+   const int nx = h->cfg.nx;
+   std::vector<uint32_t> dcell, ucounts;
    std::vector<OddTile> tiles;
-   std::vector<uint2> ucounts;
-   tiles.reserve(dcell.size() / 32 + (size_t)nrows);
-   ucounts.reserve(dcell.size() + (size_t)nrows * 32);
-   for (int64_t r = 0; r < nrows; r++) {
-      const int y = (int)(r % ny), z = (int)(r / ny);
-      int64_t nbr[9];
-      for (int k = 0; k < 9; k++) {
-         const int yy = (y + k / 3 - 1 + ny) % ny, zz = (z + k % 3 - 1 + nz) % nz;
-         nbr[k] = (int64_t)yy + (int64_t)ny * zz;
-      }
-      const uint32_t start = rstart[(size_t)r], cnt = rcount[(size_t)r];
-      uint32_t q = 0;
-      while (q < cnt) {
-         const int xa = (int)(dcell[start + q] - (uint32_t)(r * nx));
-         OddTile t{};
-         for (int k = 0; k < 9; k++) {
-            const int64_t rk = nbr[k];
-            t.b[k] = rstart[(size_t)rk] + pre[(size_t)(rk * nx + xa)];
-            t.n[k] = rcount[(size_t)rk];
-         }
-         uint32_t m = 0;
-         while (m < 32 && q + m < cnt) {
-            const int x = (int)(dcell[start + q + m] - (uint32_t)(r * nx));
-            if (x - xa > 255) break;
-            uint32_t w[2] = {0u, 0u};
-            int byte = 0;
-            for (int k = 0; k < 9; k++) {
-               if (k == 4) continue;
-               const int64_t rk = nbr[k];
-               const uint32_t uk = (uint32_t)pre[(size_t)(rk * nx + x)] - pre[(size_t)(rk * nx + xa)];
-               w[byte / 4] |= uk << (8 * (byte % 4));
-               byte++;
-            }
-            ucounts.push_back(make_uint2(w[0], w[1]));
-            m++;
-         }
-         t.ncell = m;
-         for (uint32_t l = m; l < 32; l++) ucounts.push_back(make_uint2(0u, 0u));
-         tiles.push_back(t);
-         q += m;
-      }
-   }
+   build_row_tiles(nx, h->cfg.ny, h->cfg.nz, solid, dcell, tiles, ucounts);
    free_compact(h);
    h->nf32 = (uint32_t)dcell.size();
    h->cplane = (h->nf32 + 255u) / 256u * 256u;
@@ -415,8 +354,8 @@ lbm_status build_compact(lbm_handle* h, const uint8_t* solid)
       size_t bytes;
    } parts[4] = {{(void**)&h->dcell, dcell.data(), 4 * dcell.size()},
                  {(void**)&h->ctiles, tiles.data(), sizeof(OddTile) * tiles.size()},
-                 {(void**)&h->cu, ucounts.data(), sizeof(uint2) * ucounts.size()},
-                 {(void**)&h->clk, nullptr, 4 * ucounts.size()}};
+                 {(void**)&h->cu, ucounts.data(), sizeof(uint32_t) * ucounts.size()},
+                 {(void**)&h->clk, nullptr, 2 * ucounts.size()}};
    for (int k = 0; k < 4; k++) {
       const size_t bytes = std::max<size_t>(parts[k].bytes, 16);
       lbm_status st = dev_alloc(h, parts[k].dst, bytes);

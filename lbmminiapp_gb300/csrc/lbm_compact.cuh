@@ -24,18 +24,10 @@
 
 #include <cstdint>
 
+#include "lbm_compact_tiles.hh"
 #include "lbm_physics.cuh"
 
 namespace lbm {
-
-// Row tile of the odd step, 80 bytes (five 16-byte copies).
-struct OddTile {
-   uint32_t b[9];       // compact index of the first fluid cell at or after xa in row k = 3 (dy + 1) + (dz + 1)
-   uint32_t n[9];       // fluid cells in row k
-   uint32_t ncell;      // fluid cells in the tile (1..32)
-   uint32_t pad;
-};
-static_assert(sizeof(OddTile) == 80, "OddTile is five 16-byte words");
 
 // Link-word bits of a compact cell beyond the direction bits (Q <= 27) and
 // kSolidBit (a tile lane without a cell): the cell sits at x = 0 / x = nx - 1.
