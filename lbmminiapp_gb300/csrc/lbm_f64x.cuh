@@ -693,74 +693,74 @@ __host__ __device__ __forceinline__ bool collide_f64x_fast_emit(const uint64_t (
          cu = {u3.h, fadd(u3.l, fadd(cu.l, tz.l))};
          pair(18 + j, 25 - j, 1, ny ? -1 : 1, nz ? -1 : 1, cu, owr[3], k.om2w[3]);
       }
-      return range.ok();
-   }
+   } else {
 #pragma unroll
-   for (int q = 0; q < NP; q++) {
-      const int s = pair_dir(Q, q), o = lat_opp(Q, s);
-      const int c0 = lat_c(Q, s, 0), c1 = lat_c(Q, s, 1), c2 = lat_c(Q, s, 2);
-      const int cls = lat_norm2(Q, s);
-      // cu = 3 c_s.v (two_sum-based, left unnormalised)
-      df cu = {0.f, 0.f};
-      bool first = true;
-      if (c0 != 0) { cu = c0 > 0 ? v3[0] : df_neg(v3[0]); first = false; }
-      if (c1 != 0) {
-         const df t = c1 > 0 ? v3[1] : df_neg(v3[1]);
-         if (first) { cu = t; first = false; }
-         else { const df u2 = two_sum(cu.h, t.h); cu = {u2.h, fadd(u2.l, fadd(cu.l, t.l))}; }
-      }
-      if (c2 != 0) {
-         const df t = c2 > 0 ? v3[2] : df_neg(v3[2]);
-         if (first) { cu = t; first = false; }
-         else { const df u2 = two_sum(cu.h, t.h); cu = {u2.h, fadd(u2.l, fadd(cu.l, t.l))}; }
-      }
-      // Qp = base + cu^2 / 2
-      const df c2h = df_sqr_u(cu);
-      const df qs = fast_two_sum(base.h, 0.5f * c2h.h);
-      const df Qp = {qs.h, fadd(qs.l, fadd(base.l, 0.5f * c2h.l))};
-      df A = df_mul_u(owr[cls], Qp);   // omega * eq, symmetric part
-      df B = df_mul_u(owr[cls], cu);   // omega * eq, antisymmetric part
-      // forcing om2 w (+-cf - fu + cu cf) = +-Kf[s] + (Kf[s] cu - om2 w fu), with
-      // Kf[s] = om2 w cf a float pair made on the host
-      df sym = {0.f, 0.f};
-      if (FORCE) {
-         const df gc = df_mul_u(k.Kf[s], cu);
-         const df wf = df_mul_u(k.om2w[cls], fu);
-         const df t3 = two_sum(gc.h, -wf.h);
-         sym = {t3.h, fadd(t3.l, fsub(gc.l, wf.l))};
-      }
-      if (FORCE == 2) {
-         // small force: sym joins the symmetric part (far below it) and
-         // Kf[s] the antisymmetric part (which may vanish, hence TwoSum)
-         const df as = fast_two_sum(A.h, sym.h);
-         A = {as.h, fadd(as.l, fadd(A.l, sym.l))};
-         const df bs = two_sum(B.h, k.Kf[s].h);
-         B = {bs.h, fadd(bs.l, fadd(B.l, k.Kf[s].l))};
-      }
-      // s: A + B ; opp(s): A - B ; then + (1 - omega) f
-      {
-         const df tp = fast_two_sum(A.h, B.h);
-         const df a = df_mul_u(k.om1, input_pair(f, again, s));
-         const df t = two_sum(tp.h, a.h);
-         df out = {t.h, fadd(t.l, fadd(tp.l, fadd(fadd(A.l, B.l), a.l)))};
-         if (FORCE == 1) {
-            const df fr = two_sum(k.Kf[s].h, sym.h);
-            const df t2 = two_sum(out.h, fr.h);
-            out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fadd(k.Kf[s].l, sym.l))))};
+      for (int q = 0; q < NP; q++) {
+         const int s = pair_dir(Q, q), o = lat_opp(Q, s);
+         const int c0 = lat_c(Q, s, 0), c1 = lat_c(Q, s, 1), c2 = lat_c(Q, s, 2);
+         const int cls = lat_norm2(Q, s);
+         // cu = 3 c_s.v (two_sum-based, left unnormalised)
+         df cu = {0.f, 0.f};
+         bool first = true;
+         if (c0 != 0) { cu = c0 > 0 ? v3[0] : df_neg(v3[0]); first = false; }
+         if (c1 != 0) {
+            const df t = c1 > 0 ? v3[1] : df_neg(v3[1]);
+            if (first) { cu = t; first = false; }
+            else { const df u2 = two_sum(cu.h, t.h); cu = {u2.h, fadd(u2.l, fadd(cu.l, t.l))}; }
          }
-         emit(s, join(out, range));
-      }
-      {
-         const df tm = fast_two_sum(A.h, -B.h);
-         const df a = df_mul_u(k.om1, input_pair(f, again, o));
-         const df t = two_sum(tm.h, a.h);
-         df out = {t.h, fadd(t.l, fadd(tm.l, fadd(fsub(A.l, B.l), a.l)))};
-         if (FORCE == 1) {
-            const df fr = two_sum(sym.h, -k.Kf[s].h);
-            const df t2 = two_sum(out.h, fr.h);
-            out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fsub(sym.l, k.Kf[s].l))))};
+         if (c2 != 0) {
+            const df t = c2 > 0 ? v3[2] : df_neg(v3[2]);
+            if (first) { cu = t; first = false; }
+            else { const df u2 = two_sum(cu.h, t.h); cu = {u2.h, fadd(u2.l, fadd(cu.l, t.l))}; }
          }
-         emit(o, join(out, range));
+         // Qp = base + cu^2 / 2
+         const df c2h = df_sqr_u(cu);
+         const df qs = fast_two_sum(base.h, 0.5f * c2h.h);
+         const df Qp = {qs.h, fadd(qs.l, fadd(base.l, 0.5f * c2h.l))};
+         df A = df_mul_u(owr[cls], Qp);   // omega * eq, symmetric part
+         df B = df_mul_u(owr[cls], cu);   // omega * eq, antisymmetric part
+         // forcing om2 w (+-cf - fu + cu cf) = +-Kf[s] + (Kf[s] cu - om2 w fu), with
+         // Kf[s] = om2 w cf a float pair made on the host
+         df sym = {0.f, 0.f};
+         if (FORCE) {
+            const df gc = df_mul_u(k.Kf[s], cu);
+            const df wf = df_mul_u(k.om2w[cls], fu);
+            const df t3 = two_sum(gc.h, -wf.h);
+            sym = {t3.h, fadd(t3.l, fsub(gc.l, wf.l))};
+         }
+         if (FORCE == 2) {
+            // small force: sym joins the symmetric part (far below it) and
+            // Kf[s] the antisymmetric part (which may vanish, hence TwoSum)
+            const df as = fast_two_sum(A.h, sym.h);
+            A = {as.h, fadd(as.l, fadd(A.l, sym.l))};
+            const df bs = two_sum(B.h, k.Kf[s].h);
+            B = {bs.h, fadd(bs.l, fadd(B.l, k.Kf[s].l))};
+         }
+         // s: A + B ; opp(s): A - B ; then + (1 - omega) f
+         {
+            const df tp = fast_two_sum(A.h, B.h);
+            const df a = df_mul_u(k.om1, input_pair(f, again, s));
+            const df t = two_sum(tp.h, a.h);
+            df out = {t.h, fadd(t.l, fadd(tp.l, fadd(fadd(A.l, B.l), a.l)))};
+            if (FORCE == 1) {
+               const df fr = two_sum(k.Kf[s].h, sym.h);
+               const df t2 = two_sum(out.h, fr.h);
+               out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fadd(k.Kf[s].l, sym.l))))};
+            }
+            emit(s, join(out, range));
+         }
+         {
+            const df tm = fast_two_sum(A.h, -B.h);
+            const df a = df_mul_u(k.om1, input_pair(f, again, o));
+            const df t = two_sum(tm.h, a.h);
+            df out = {t.h, fadd(t.l, fadd(tm.l, fadd(fsub(A.l, B.l), a.l)))};
+            if (FORCE == 1) {
+               const df fr = two_sum(sym.h, -k.Kf[s].h);
+               const df t2 = two_sum(out.h, fr.h);
+               out = {t2.h, fadd(t2.l, fadd(out.l, fadd(fr.l, fsub(sym.l, k.Kf[s].l))))};
+            }
+            emit(o, join(out, range));
+         }
       }
    }
    return range.ok();
